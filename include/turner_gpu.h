@@ -1,0 +1,239 @@
+/*
+ * turner_gpu.h — C ABI of the GB300 path-tracing core.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes, no
+ * exceptions and no C++ or torch types cross it. One context owns device
+ * memory and one CUDA stream on one GPU; calls on a context come from one
+ * host thread at a time.
+ *
+ * What it replaces in the reference (turner-renderer/turner):
+ *   - the render block of main.cpp:181-236 (row thread pool, pixel/sample
+ *     loops, per-pixel mean, exposure, gamma) together with the per-ray
+ *     renderer plug-in `Color trace(const Ray&, KDTreeIntersection&,
+ *     const std::vector<Light>&, int depth, const TracerConfig&)`
+ *     (trace.h:23-25, defined in pathtracer.cpp:14-102)   -> turner_render
+ *   - `const OptionalId KDTreeIntersection::intersect(const Ray&, float& r,
+ *     float& a, float& b)` (lib/kdtree.h:291, lib/kdtree.cpp:516-607),
+ *     batched                                             -> turner_intersect
+ *   - the kd-tree produced by `KDTree::KDTree(Triangles)` (lib/kdtree.cpp:474-490)
+ *     is consumed verbatim: FlatNode words and the precomputed Triangle fields,
+ *     in the order KDTree::serialize / Triangle::serialize emit them
+ *     (lib/kdtree.h:228-230, lib/triangle.h:89-92)        -> turner_upload_scene
+ *   - `KDTree::KDTree(Triangles)` itself, re-implemented on the host with the
+ *     same node output                                   -> turner_kdtree_build
+ */
+#ifndef TURNER_GPU_H
+#define TURNER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define TURNER_OK 0
+#define TURNER_ERR_INVALID_ARG (-1)   /* null pointer, zero size, bad enum      */
+#define TURNER_ERR_CUDA (-2)          /* a CUDA runtime call failed             */
+#define TURNER_ERR_OUT_OF_MEMORY (-3) /* device or host allocation failed       */
+#define TURNER_ERR_BAD_SCENE (-4)     /* node array fails validation            */
+#define TURNER_ERR_TIMEOUT (-5)       /* a bounded device wait gave up          */
+#define TURNER_ERR_DEVICE_BOUNDS (-6) /* a device-side index check fired        */
+#define TURNER_ERR_UNSUPPORTED (-7)   /* valid but not implemented combination  */
+#define TURNER_ERR_NO_DEVICE (-8)     /* no CUDA device / wrong architecture    */
+#define TURNER_ERR_TOO_LARGE (-9)     /* request exceeds a documented maximum   */
+
+/* Triangle id returned for a miss: detail::OptionalId's invalid value
+ * FlatNode::MAX_TRIANGLE_ID = 1 << 30 (lib/kdtree.h:66,156-160). */
+#define TURNER_MISS 0x40000000u
+
+/* Pointer placement flags for turner_intersect / turner_render. */
+#define TURNER_HOST_BUFFERS 0u   /* arrays are host memory; copies are made  */
+#define TURNER_DEVICE_BUFFERS 1u /* arrays are device memory of this context's GPU */
+
+/* Traversal modes. PARITY reproduces KDTreeIntersection::intersect exactly:
+ * every overlapped leaf is visited, first strict minimum kept. FAST stops
+ * once no later cell can hold a closer hit (checked against PARITY by the
+ * tests). Shadow rays always stop at the first blocker; that is exact. */
+#define TURNER_TRAVERSAL_PARITY 0
+#define TURNER_TRAVERSAL_FAST 1
+
+/* Bounce sampling. UNIFORM is the reference's sampling::hemisphere
+ * (lib/sampling.h:20-32, weight 2*cos); COSINE is cosine-weighted. */
+#define TURNER_SAMPLING_UNIFORM 0
+#define TURNER_SAMPLING_COSINE 1
+
+/* ------------------------------------------------------------- records */
+
+/* One triangle in Triangle::serialize order (lib/triangle.h:89-114):
+ * 48 floats = 192 bytes. `u`, `v`, `normal`, `uv`, `vv`, `uu`, `denom` are
+ * the constructor's precomputed values (lib/triangle.h:22-39); pass them as
+ * the reference computed them for bit-exact hits. */
+typedef struct turner_triangle {
+    float vertices[3][3];
+    float normals[3][3];
+    float ambient[4];
+    float diffuse[4];
+    float emissive[4];
+    float reflective[4];
+    float reflectivity;
+    float u[3];
+    float v[3];
+    float normal[3];
+    float uv, vv, uu, denom;
+} turner_triangle;
+
+/* Pinhole camera of lib/types.h:88-123. The camera looks down -z of its node
+ * frame; `trafo` is the node's rotation (row-major a1..c3), `position` the
+ * node's translation. Primary directions are NOT normalised (raster2cam). */
+typedef struct turner_camera {
+    float position[3];
+    float trafo[9];
+    float delta_x; /* tan(aiCamera::mHorizontalFOV), as Camera computes it */
+    float aspect;  /* aiCamera::mAspect; delta_y = delta_x / aspect        */
+} turner_camera;
+
+/* Point light (lib/types.h:81-84). No distance falloff, as in the reference. */
+typedef struct turner_light {
+    float position[3];
+    float color[4];
+} turner_light;
+
+/* One image to render: the TracerConfig fields of config.h:13-165 that the
+ * path tracer reads, plus the scene, camera, light and seed. */
+typedef struct turner_job {
+    uint32_t scene_id;
+    uint32_t width;               /* -w                                       */
+    uint32_t height;              /* the reference uses int(width / aspect)   */
+    uint32_t pixel_samples;       /* -p                                       */
+    int32_t max_depth;            /* -d: rays are traced at depths 0..max_depth */
+    int32_t monte_carlo_samples;  /* -m: 0 or 1 (the branching estimator of -m>1
+                                     is not implemented: TURNER_ERR_UNSUPPORTED) */
+    float exposure;               /* --exposure                               */
+    float inverse_gamma;          /* --inverse-gamma                          */
+    int32_t gamma_correction;     /* 0 for --no-gamma-correction              */
+    float background[3];          /* --background; alpha is 1                 */
+    uint64_t seed;                /* per-(pixel, sample) stream seed base     */
+    int32_t n_lights;             /* 0 or 1 (main.cpp:121-136 allows at most 1) */
+    turner_light light;
+    turner_camera camera;
+    int32_t sampling;             /* TURNER_SAMPLING_*                        */
+    int32_t traversal;            /* TURNER_TRAVERSAL_* for bounce rays       */
+} turner_job;
+
+typedef struct turner_stats {
+    uint64_t rays;          /* reference count: traced rays at depth <= max_depth,
+                               misses included, shadow rays excluded (pathtracer.cpp:21) */
+    uint64_t primary_rays;  /* main.cpp:211                                */
+    uint64_t shadow_rays;   /* one per hit with a light                    */
+    double device_ms;       /* device time of the render, CUDA events      */
+} turner_stats;
+
+typedef struct turner_ctx turner_ctx;
+typedef struct turner_kdtree turner_kdtree;
+typedef struct turner_mesh turner_mesh;
+
+/* ------------------------------------------------------------ context */
+const char* turner_strerror(int status);
+int turner_create(turner_ctx** out, int device);
+void turner_destroy(turner_ctx* ctx);
+/* Last device-side error word (TURNER_ERR_* or 0) and clears it. */
+int turner_last_device_error(turner_ctx* ctx);
+
+/* --------------------------------------------------------------- scene */
+/* Copies a flattened kd-tree to the device. `nodes` are FlatNode::data_
+ * words (lib/kdtree.h:136-153) in the reference's DFS order; `box` is
+ * KDTree::box() as {min x,y,z, max x,y,z}. The node array is validated on
+ * the host (child indices forward and in range, leaf ids < n_tris, every
+ * leaf run terminated inside the array) so that device traversal is in
+ * bounds by construction; a failing array returns TURNER_ERR_BAD_SCENE. */
+int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes, const turner_triangle* tris,
+                        uint32_t n_tris, const float box[6], uint32_t* scene_id);
+int turner_free_scene(turner_ctx* ctx, uint32_t scene_id);
+
+/* ---------------------------------------------------------- intersect */
+/* Batched KDTreeIntersection::intersect. Rays are SoA (ox, oy, oz, dx, dy,
+ * dz), each of n floats; directions need not be normalised. For each ray:
+ * hit_id = triangle index or TURNER_MISS; r = parametric distance (FLT_MAX on
+ * a miss); s, t = barycentric coordinates (0 on a miss). `flags` selects
+ * host or device buffers. `mode` is TURNER_TRAVERSAL_*. Synchronous. */
+int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
+                     const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id, float* r,
+                     float* s, float* t, int mode, uint32_t flags);
+
+/* -------------------------------------------------------------- render */
+/* Renders each job into out_rgba[j] (width*height*4 floats, row-major RGBA
+ * after the per-pixel mean, exposure and gamma of main.cpp:216-223), host or
+ * device memory per `flags`. All jobs go through one wavefront launch
+ * sequence (one CUDA graph when n_jobs > 1). stats may be NULL; otherwise it
+ * receives one turner_stats per job. Synchronous. */
+int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float* const* out_rgba,
+                  turner_stats* stats, uint32_t flags);
+
+/* Progressive FP64 accumulation for converged reference images: adds
+ * `passes` further sample passes of pixel_samples each to a double-precision
+ * per-pixel sum held by the context (keyed by job seed and size) and writes
+ * the running mean (linear radiance, no tone map) to out_rgba. */
+int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t passes, double* out_rgba_mean,
+                             uint64_t* total_samples, uint32_t flags);
+
+/* ---------------------------------------------------------- host tree */
+/* SAH kd-tree of [WH06] Algorithm 4 with the reference's constants and
+ * tie-breaking (lib/kdtree.cpp:124-467): the node words and triangle records
+ * are identical to KDTree's. vertices: n*9 floats (v0, v1, v2); normals: n*9
+ * or NULL (zero normals); diffuse: n*4 or NULL. Subtrees are built on
+ * `threads` host threads (0 = all cores). */
+int turner_kdtree_build(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris,
+                        int threads, turner_kdtree** out);
+uint32_t turner_kdtree_num_nodes(const turner_kdtree* tree);
+uint32_t turner_kdtree_num_triangles(const turner_kdtree* tree);
+uint32_t turner_kdtree_height(const turner_kdtree* tree);
+/* Copies nodes (num_nodes words), triangle records and box out; any may be NULL. */
+int turner_kdtree_export(const turner_kdtree* tree, uint64_t* nodes, turner_triangle* tris, float box[6]);
+int turner_upload_kdtree(turner_ctx* ctx, const turner_kdtree* tree, uint32_t* scene_id);
+void turner_kdtree_free(turner_kdtree* tree);
+
+/* ------------------------------------------------------------ scenes */
+/* Seeded synthetic scenes (the reference loads .blend files through assimp,
+ * which this build does not ship):
+ *   0 ROOM         36-triangle box room: 5 walls, two boxes rotated +-17 deg,
+ *                  a 2-triangle ceiling quad, point light below the ceiling
+ *   1 SPHERE_ROOM  room shell + icosphere subdivided `detail` times (7 ->
+ *                  327,680 triangles), displaced by 5-octave value noise
+ *   2 SOUP         clustered triangle soup of `count` triangles in the room
+ *   3 BAFFLE_ROOM  walls tessellated detail x detail quads, a 1.5x1.5 baffle
+ *                  0.3 below the light
+ *   4 BAFFLE_SPHERE the SPHERE_ROOM sphere inside the BAFFLE_ROOM room */
+#define TURNER_SCENE_ROOM 0
+#define TURNER_SCENE_SPHERE_ROOM 1
+#define TURNER_SCENE_SOUP 2
+#define TURNER_SCENE_BAFFLE_ROOM 3
+#define TURNER_SCENE_BAFFLE_SPHERE 4
+
+int turner_scene_make(int kind, uint32_t detail, uint32_t count, uint64_t seed, float aspect, turner_mesh** out);
+uint32_t turner_mesh_num_triangles(const turner_mesh* mesh);
+const float* turner_mesh_vertices(const turner_mesh* mesh); /* n*9 */
+const float* turner_mesh_normals(const turner_mesh* mesh);  /* n*9 */
+const float* turner_mesh_diffuse(const turner_mesh* mesh);  /* n*4 */
+/* Camera as the scene defines it; *hfov receives aiCamera::mHorizontalFOV. */
+void turner_mesh_camera(const turner_mesh* mesh, turner_camera* cam, float* hfov);
+/* Returns the number of lights (0 or 1) and copies the first. */
+int turner_mesh_light(const turner_mesh* mesh, turner_light* light);
+void turner_mesh_free(turner_mesh* mesh);
+
+/* Hit-test ray set: n rays, origins uniform in box, directions uniform on
+ * the sphere (Marsaglia 1972), seeded; SoA outputs of n floats each. */
+int turner_make_rays(uint64_t n, const float box[6], uint64_t seed, float* ox, float* oy, float* oz, float* dx,
+                     float* dy, float* dz);
+
+/* --------------------------------------------------------------- output */
+/* P3 writer of lib/raster.h:79-100. Returns the byte length of the full
+ * text; writes at most `cap` bytes to `out` (which may be NULL). */
+uint64_t turner_write_p3(const float* rgba, uint32_t width, uint32_t height, char* out, uint64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TURNER_GPU_H */
