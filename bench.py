@@ -1,0 +1,339 @@
+"""Benchmark: Mrays/s of the GB300 path tracer on the large-mesh workload.
+
+Workload (one "step" = one full frame): the 327,692-triangle scene (icosphere
+subdivided 7 times, radius 1.5, 5-octave value-noise displacement, amplitude
+0.08, base frequency 4, inside the open-front box room), 1920x1080, 16 pixel
+samples, max depth 3, 1 Monte Carlo sample per bounce, one point light.
+Synthetic, seeded geometry; the tree is the reference's SAH kd-tree (built on
+the host, identical node words).
+
+Metric: Mrays/s with the reference's ray count (pathtracer.cpp:21: traced rays
+at depth <= max depth, misses included, shadow rays excluded).
+
+  value   frame time on the device (CUDA events on the library's stream) with
+          the scene resident in HBM, output image in device memory
+  e2e     the same through the public C ABI with host buffers: the scene is
+          uploaded from host memory, rendered and the image read back, every
+          step (turner_upload_scene + turner_render + turner_free_scene)
+
+`--impl reference` times the reference's CPU path tracer (the oracle
+restatement of pathtracer.cpp / kdtree.cpp, all host threads) on a bounded
+band of rows of the same frame.
+
+Multi-GPU (torchrun, one rank per GPU): frames are independent objects; every
+rank renders its own frame (different seed), no collective on the data path;
+scaling is weak and value = all ranks' rays / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WIDTH, HEIGHT, SPP, DEPTH, MC = 1920, 1080, 16, 3, 1
+WORKLOAD = "sphere_room_327k_1920x1080_16spp_d3"
+METRIC = "Mrays/s (reference ray count: primary + bounce rays incl. misses, excl. shadow rays)"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+TRAFFIC = ROOT / "profiles" / "k_trace_traffic.json"
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def sample_clocks(stop: threading.Event, out: list, device: int):
+    q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                              "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append(line.strip())
+    finally:
+        p.terminate()
+        try:
+            p.wait(timeout=2)
+        except subprocess.TimeoutExpired:
+            p.kill()
+
+
+def summarize_clocks(lines: list[str]) -> dict:
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        parts = [x.strip() for x in ln.split(",")]
+        if len(parts) < 7:
+            continue
+        try:
+            sm.append(float(parts[0]))
+            mx.append(float(parts[1]))
+        except ValueError:
+            continue
+        for name, val in zip(names, parts[3:7]):
+            if val.lower() == "active":
+                reasons.add(name)
+    if not sm:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload():
+    import turner_gb300 as tg
+
+    mesh = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=7, aspect=16 / 9)
+    t0 = time.perf_counter()
+    tree = tg.KDTree.from_mesh(mesh)
+    build_s = time.perf_counter() - t0
+    return mesh, tree, build_s
+
+
+def cpu_baseline(mesh, tree, seed: int, budget_s: float = 12.0, band: int = 8):
+    """Oracle render of whole rows of the same frame, all host threads, until
+    about budget_s of wall time; returns (Mrays/s, rows, stats)."""
+    from oracle import oracle as orc
+
+    nodes, tris, box = tree.export()
+    sc = orc.Scene(nodes, tris, box)
+    threads = os.cpu_count() or 1
+    y0 = HEIGHT // 2 - band // 2
+    rays = 0
+    stats = np.zeros(7, np.uint64)
+    rows = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and rows < HEIGHT:
+        a = (y0 + rows) % HEIGHT
+        b = min(a + band, HEIGHT)
+        _, st = sc.render(mesh.camera, mesh.light, WIDTH, HEIGHT, SPP, DEPTH, mc=MC, seed=seed, threads=threads,
+                          rows=(a, b))
+        stats += st
+        rows += b - a
+    dt = time.perf_counter() - t0
+    return float(stats[0]) / dt / 1e6, rows, stats, threads, dt
+
+
+def run_reference(args) -> None:
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    import turner_gb300 as tg  # scene generation and the host tree only
+
+    mesh, tree, _ = make_workload()
+    from oracle import oracle as orc
+
+    nodes, tris, box = tree.export()
+    sc = orc.Scene(nodes, tris, box)
+    threads = os.cpu_count() or 1
+    band = args.ref_rows
+    y0 = HEIGHT // 2 - band // 2
+
+    def step(i):
+        _, st = sc.render(mesh.camera, mesh.light, WIDTH, HEIGHT, SPP, DEPTH, mc=MC, seed=1 + i, threads=threads,
+                          rows=(y0, y0 + band))
+        return int(st[0])
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    rays = sum(step(i) for i in range(args.steps))
+    dt = time.perf_counter() - t0
+    value = rays / dt / 1e6
+    sample = f"rows {y0}-{y0 + band} of the {WIDTH}x{HEIGHT} frame ({band * WIDTH * SPP} paths per step)"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample, "threads": threads},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--traversal", default="parity", choices=["parity", "fast"])
+    ap.add_argument("--chunk-paths", type=int, default=1 << 24)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--ref-rows", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, world, local = rank_info()
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+
+    import turner_gb300 as tg
+
+    mesh, tree, build_s = make_workload()
+    ctx = tg.Context(device)
+    ctx.set_chunk_paths(args.chunk_paths)
+    sid = ctx.upload_tree(tree)
+    nodes, tris, box = tree.export()
+    traversal = tg.TRAVERSAL_FAST if args.traversal == "fast" else tg.TRAVERSAL_PARITY
+    seed = 1 + rank
+    job = tg.make_job(sid, mesh, WIDTH, HEIGHT, pixel_samples=SPP, max_depth=DEPTH, monte_carlo_samples=MC,
+                      seed=seed, traversal=traversal)
+    out = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32, device=f"cuda:{device}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")   # > L2 (126 MiB)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    for _ in range(args.warmup):
+        ctx.render([job], [out.data_ptr()], tg.DEVICE_BUFFERS)
+
+    # timed, device-resident: L2 flushed between steps (outside the timed kernels)
+    ctx.set_profiling(True)
+    ctx.kernel_times(reset=True)
+    launches0 = ctx.launch_count()
+    clock_lines: list[str] = []
+    stop = threading.Event()
+    sampler = threading.Thread(target=sample_clocks, args=(stop, clock_lines, device), daemon=True)
+    sampler.start()
+    barrier()
+    t0 = time.perf_counter()
+    dev_ms, rays, shadow = 0.0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        _, (st,) = ctx.render([job], [out.data_ptr()], tg.DEVICE_BUFFERS)
+        dev_ms += st.device_ms
+        rays += st.rays
+        shadow += st.shadow_rays
+    barrier()
+    wall = time.perf_counter() - t0
+    stop.set()
+    sampler.join(timeout=5)
+    launches = ctx.launch_count() - launches0
+    ktimes = ctx.kernel_times(reset=True)
+    ctx.set_profiling(False)
+
+    # end to end through the C ABI with host buffers
+    img_host = np.empty((HEIGHT, WIDTH, 4), np.float32)
+    h2d = nodes.nbytes + 2 * 64 * tris.shape[0]   # node words + intersection and shading records
+    d2h = img_host.nbytes
+    barrier()
+    e0 = time.perf_counter()
+    e_rays = 0
+    for _ in range(args.steps):
+        s2 = ctx.upload(nodes, tris, box)
+        j2 = tg.make_job(s2, mesh, WIDTH, HEIGHT, pixel_samples=SPP, max_depth=DEPTH, monte_carlo_samples=MC,
+                         seed=seed, traversal=traversal)
+        (img,), (st,) = ctx.render([j2])
+        e_rays += st.rays
+        ctx.free_scene(s2)
+    barrier()
+    e_wall = time.perf_counter() - e0
+
+    t_max = dev_ms / 1000.0
+    if dist is not None:
+        t = torch.tensor([t_max, e_wall], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max, e_wall = float(t[0]), float(t[1])
+        r = torch.tensor([rays, e_rays], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(r, op=dist.ReduceOp.SUM)
+        rays_all, e_rays_all = float(r[0]), float(r[1])
+    else:
+        rays_all, e_rays_all = float(rays), float(e_rays)
+    value = rays_all / t_max / 1e6
+
+    result = None
+    if rank == 0:
+        # roofline of the dominant kernel (closest-hit traversal): algorithmic
+        # bytes per ray from the oracle's count of the reference's traversal
+        # (every overlapped leaf, no early exit) on the CPU sample of this frame
+        peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        cpu = None
+        visits_per_ray = tests_per_ray = None
+        if not args.no_cpu:
+            cpu_mrays, cpu_rows, cst, threads, cdt = cpu_baseline(mesh, tree, seed, budget_s=args.cpu_budget)
+            visits_per_ray = float(cst[3]) / float(cst[0])
+            tests_per_ray = float(cst[4]) / float(cst[0])
+            cpu = {"value": round(cpu_mrays, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                   "sample": f"{cpu_rows} full rows of the same frame ({cpu_rows * WIDTH * SPP} paths, "
+                             f"{cdt:.1f} s, oracle restatement of the reference, all host threads)"}
+        kt_ms, kt_n = ktimes["k_trace"]
+        dominant = max(ktimes, key=lambda k: ktimes[k][0])
+        roof = None
+        if visits_per_ray is not None and kt_ms > 0:
+            bytes_per_ray = 8 * visits_per_ray + 64 * tests_per_ray + 32 + 16
+            per_launch_bytes = bytes_per_ray * rays / max(kt_n, 1)
+            avg_launch_s = kt_ms / 1000.0 / max(kt_n, 1)
+            achieved = per_launch_bytes / avg_launch_s / 1e9
+            traffic = None
+            if TRAFFIC.exists():
+                tr = json.loads(TRAFFIC.read_text())
+                traffic = tr.get("dram_bytes_per_ray", 0) * rays / max(kt_n, 1)
+            roof = {"kernel": "k_trace", "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                    "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic,
+                    "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if PEAKS.exists() else "fallback",
+                    "bytes_per_ray": round(bytes_per_ray, 1), "node_visits_per_ray": round(visits_per_ray, 2),
+                    "triangle_tests_per_ray": round(tests_per_ray, 2)}
+        clocks = summarize_clocks(clock_lines)
+        result = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000 * t_max / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "nodes": int(nodes.size),
+                       "width": WIDTH, "height": HEIGHT, "pixel_samples": SPP, "max_depth": DEPTH,
+                       "monte_carlo_samples": MC, "traversal": args.traversal, "chunk_paths": args.chunk_paths,
+                       "l2": "flushed between steps (512 MiB write outside the timed kernels)",
+                       "parallelism": f"frames per rank x{world}" if world > 1 else "single GPU",
+                       "kdtree_build_s": round(build_s, 3)},
+            "e2e": {"value": round(e_rays_all / e_wall / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "rays_per_step": int(rays // args.steps), "shadow_rays_per_step": int(shadow // args.steps),
+            "wall_ms_per_step": round(1000 * wall / args.steps, 3),
+            "kernels_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in ktimes.items() if v[1]},
+            "dominant_kernel": dominant,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(result))
+    ctx.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -140,6 +140,30 @@ int turner_create(turner_ctx** out, int device);
 void turner_destroy(turner_ctx* ctx);
 /* Last device-side error word (TURNER_ERR_* or 0) and clears it. */
 int turner_last_device_error(turner_ctx* ctx);
+/* Text of the last failing CUDA call on this context ("" if none). No
+ * reference counterpart: diagnostics of this library. */
+const char* turner_last_error_message(turner_ctx* ctx);
+/* Number of kernels this context has launched so far. No reference
+ * counterpart: lets benchmarks report how much work ran on the GPU. */
+uint64_t turner_launch_count(turner_ctx* ctx);
+/* Paths in flight per render pass (queue length), >= 1024. Default 2^24.
+ * No reference counterpart: the reference renders one row per task. */
+int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths);
+
+/* Per-kernel device time, measured with CUDA events on the context stream
+ * around every launch while profiling is on. No reference counterpart: the
+ * reference only has Runtime wall-clock timers (lib/runtime.h). */
+#define TURNER_KERNEL_CAMERA 0
+#define TURNER_KERNEL_TRACE 1     /* closest-hit traversal of a ray queue  */
+#define TURNER_KERNEL_SHADE 2
+#define TURNER_KERNEL_SHADOW 3    /* any-hit traversal of the shadow queue */
+#define TURNER_KERNEL_RESOLVE 4
+#define TURNER_KERNEL_INTERSECT 5
+#define TURNER_KERNEL_KINDS 6
+int turner_set_profiling(turner_ctx* ctx, int on);
+/* Copies the accumulated milliseconds and launch counts per kind (arrays of
+ * TURNER_KERNEL_KINDS; either may be NULL) and optionally resets them. */
+int turner_kernel_times(turner_ctx* ctx, double* ms, uint64_t* launches, int reset);
 
 /* --------------------------------------------------------------- scene */
 /* Copies a flattened kd-tree to the device. `nodes` are FlatNode::data_
@@ -151,6 +175,12 @@ int turner_last_device_error(turner_ctx* ctx);
 int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes, const turner_triangle* tris,
                         uint32_t n_tris, const float box[6], uint32_t* scene_id);
 int turner_free_scene(turner_ctx* ctx, uint32_t scene_id);
+/* The host-side check turner_upload_scene applies, without a device:
+ * TURNER_OK and the traversal stack depth the tree needs (the largest number
+ * of inner nodes on a root-to-leaf path), TURNER_ERR_BAD_SCENE, or
+ * TURNER_ERR_TOO_LARGE when that depth exceeds the kernels' stack (128).
+ * No reference counterpart: the reference trusts its own builder's output. */
+int turner_validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t* stack_depth);
 
 /* ---------------------------------------------------------- intersect */
 /* Batched KDTreeIntersection::intersect. Rays are SoA (ox, oy, oz, dx, dy,

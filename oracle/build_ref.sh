@@ -21,6 +21,7 @@ pids=()
 g++ "${FLAGS[@]}" -c "$REF/lib/kdtree.cpp" -o "$OUT/kdtree.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/geometry_prelude.cpp" -o "$OUT/geometry_prelude.o" & pids+=($!)
+g++ "${FLAGS[@]}" -c "$HERE/ref_fixtures.cpp" -o "$OUT/ref_fixtures.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
-g++ -shared -o "$OUT/libturner_ref.so" "$OUT/kdtree.o" "$OUT/ref_driver.o" "$OUT/geometry_prelude.o" -lpthread
+g++ -shared -o "$OUT/libturner_ref.so" "$OUT/kdtree.o" "$OUT/ref_driver.o" "$OUT/geometry_prelude.o" "$OUT/ref_fixtures.o" -lpthread
 echo "build_ref: wrote $OUT/libturner_ref.so"

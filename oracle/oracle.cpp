@@ -167,7 +167,8 @@ inline bool intersect_ray_box(const Ray& ray, V3 pmin, V3 pmax, float& tmin, flo
 struct Intersector {
     const Scene* sc;
     std::stack<std::tuple<const uint64_t*, float, float>> stack_;
-    uint64_t node_visits = 0, tri_tests = 0;
+    uint64_t node_visits = 0, tri_tests = 0;                // all traversals
+    uint64_t shadow_visits = 0, shadow_tests = 0;           // shadow-ray share of them
 
     explicit Intersector(const Scene& s) : sc(&s) {}
 
@@ -339,7 +340,10 @@ C4 trace(const Ray& ray, Intersector& ti, const std::vector<Light>& lights, int 
         const float dist_to_light = length(light.position - p2);
         float dist_to_next = 0, s2, t2;
         cnt.shadow_rays += 1;
+        const uint64_t v0 = ti.node_visits, t0 = ti.tri_tests;
         uint32_t sh = ti.intersect(Ray{p2, light_dir}, dist_to_next, s2, t2);
+        ti.shadow_visits += ti.node_visits - v0;
+        ti.shadow_tests += ti.tri_tests - t0;
         if (sh >= kMaxTriangleId || dist_to_next > dist_to_light) {
             direct = std::max(0.f, dot(light_dir, normal)) * light.color;
         }
@@ -472,7 +476,7 @@ void orc_intersect(void* s, const float* rays, uint64_t n, uint32_t* id, float* 
 // Render (main.cpp:181-236 with harness seeding). out_rgba: width*height*4.
 // rows [row_begin, row_end) only (row_end = 0 means all rows): bounded CPU
 // samples for the baseline. stats: [rays, primary rays, shadow rays,
-// node visits, triangle tests].
+// node visits and triangle tests of primary/bounce rays, the same of shadow rays].
 void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_rgba, uint64_t* stats,
                 int threads, uint32_t row_begin, uint32_t row_end) {
     const Scene& sc = *static_cast<Scene*>(s);
@@ -495,10 +499,10 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
     const uint32_t y_end = row_end ? std::min<uint32_t>(row_end, height) : height;
 
     std::atomic<uint32_t> next_row{row_begin};
-    std::atomic<uint64_t> n_rays{0}, n_prim{0}, n_shadow{0}, n_visits{0}, n_tests{0};
+    std::atomic<uint64_t> n_rays{0}, n_prim{0}, n_shadow{0}, n_visits{0}, n_tests{0}, n_svisits{0}, n_stests{0};
     auto work = [&]() {
         Counters cnt;
-        uint64_t prim = 0, visits = 0, tests = 0;
+        uint64_t prim = 0, visits = 0, tests = 0, svisits = 0, stests = 0;
         for (;;) {
             const uint32_t y = next_row.fetch_add(1);
             if (y >= y_end) break;
@@ -536,12 +540,16 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
             }
             visits += ti.node_visits;
             tests += ti.tri_tests;
+            svisits += ti.shadow_visits;
+            stests += ti.shadow_tests;
         }
         n_rays += cnt.rays;
         n_shadow += cnt.shadow_rays;
         n_prim += prim;
-        n_visits += visits;
-        n_tests += tests;
+        n_visits += visits - svisits;
+        n_tests += tests - stests;
+        n_svisits += svisits;
+        n_stests += stests;
     };
     if (threads < 1) threads = 1;
     std::vector<std::thread> pool;
@@ -552,6 +560,8 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
     stats[2] = n_shadow.load();
     stats[3] = n_visits.load();
     stats[4] = n_tests.load();
+    stats[5] = n_svisits.load();
+    stats[6] = n_stests.load();
 }
 
 // P3 writer (lib/raster.h:79-100): "P3\nW H\n255", then per pixel the three

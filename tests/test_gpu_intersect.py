@@ -1,0 +1,166 @@
+"""GPU closest-hit traversal == KDTreeIntersection::intersect, bit for bit.
+
+Every case goes through the C ABI (turner_intersect) and is compared with the
+CPU oracle on the same tree and rays: triangle ids equal, r, s, t equal as
+bit patterns (the kernels round like the reference's C++)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import turner_gb300 as tg
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = tg.Context(0)
+    yield c
+    c.close()
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def assert_same(gpu, ref, exact_rst=True):
+    hid, r, s, t = gpu
+    rid, rr, rs, rt = ref
+    mism = np.nonzero(hid != rid)[0]
+    assert mism.size == 0, f"{mism.size} id mismatches, first {mism[:5]}"
+    if exact_rst:
+        for a, b in ((r, rr), (s, rs), (t, rt)):
+            assert np.array_equal(bits(a), bits(b))
+
+
+SCENES = {
+    "room": dict(kind=tg.SCENE_ROOM),
+    "sphere5": dict(kind=tg.SCENE_SPHERE_ROOM, detail=5),
+    "soup20k": dict(kind=tg.SCENE_SOUP, count=20000, seed=4),
+    "baffle32": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=32),
+}
+
+
+@pytest.fixture(scope="module")
+def uploaded(ctx):
+    out = {}
+    for name, kw in SCENES.items():
+        t = tg.KDTree.from_mesh(tg.make_scene(**kw))
+        nodes, tris, box = t.export()
+        out[name] = (ctx.upload(nodes, tris, box), orc.Scene(nodes, tris, box), box)
+    return out
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_parity_random_rays(ctx, uploaded, name):
+    sid, ref, box = uploaded[name]
+    o, d = tg.make_rays(200_000, box, seed=17)
+    d[0, ::13] = 0       # fix_direction paths
+    d[2, ::19] = 0
+    assert_same(ctx.intersect(sid, o, d), ref.intersect(o, d))
+
+
+@pytest.mark.parametrize("name", ["sphere5", "soup20k"])
+def test_fast_mode_matches_parity(ctx, uploaded, name):
+    """FAST (early exit with margin) gives the same closest hit as PARITY."""
+    sid, ref, box = uploaded[name]
+    o, d = tg.make_rays(300_000, box, seed=23)
+    assert_same(ctx.intersect(sid, o, d, mode=tg.TRAVERSAL_FAST), ref.intersect(o, d))
+
+
+def test_reference_fixture_scenes(ctx):
+    """The reference's kd-tree tests (tests/test_kdtree.cpp) on the GPU."""
+    kd = dict(np.load(GOLD / "ref_kdtree_tests.npz"))
+    for name in ["four"] + [f"coplanar{a}" for a in range(3)] + [f"stacked{a}" for a in range(3)]:
+        sid = ctx.upload(kd[f"{name}_nodes"], kd[f"{name}_tris"], kd[f"{name}_box"])
+        hid, r, s, t = ctx.intersect(sid, kd[f"{name}_rays_o"], kd[f"{name}_rays_d"])
+        assert np.array_equal(hid, kd[f"{name}_hit_i"]), name
+        for k, v in zip("rst", (r, s, t)):
+            gold = kd[f"{name}_hit_{k}"]
+            hit = hid != tg.MISS
+            assert np.array_equal(bits(v)[hit], bits(gold)[hit]), (name, k)
+    # four separated triangles: exact known answers (test_kdtree.cpp:34-62)
+    sid = ctx.upload(kd["four_nodes"], kd["four_tris"], kd["four_box"])
+    hid, r, s, t = ctx.intersect(sid, kd["four_rays_o"], kd["four_rays_d"])
+    assert hid.tolist() == [0, 1, 2, 3] and (r == 1).all() and s.tolist() == [0.5, 0, 0, 0] and (t == 0.5).all()
+
+
+def test_golden_scene_rays(ctx):
+    """GPU hits == the reference's recorded hits (tests/golden/ref_scenes.npz)."""
+    g = dict(np.load(GOLD / "ref_scenes.npz"))
+    for name, kw in {"room": dict(kind=tg.SCENE_ROOM), "sphere3": dict(kind=tg.SCENE_SPHERE_ROOM, detail=3),
+                     "soup2000": dict(kind=tg.SCENE_SOUP, count=2000, seed=7),
+                     "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8)}.items():
+        sid = ctx.upload_tree(tg.KDTree.from_mesh(tg.make_scene(**kw)))
+        hid, r, s, t = ctx.intersect(sid, g[f"{name}_rays_o"], g[f"{name}_rays_d"])
+        assert np.array_equal(hid, g[f"{name}_hit_i"]), name
+        for k, v in zip("rst", (r, s, t)):
+            assert np.array_equal(bits(v), bits(g[f"{name}_hit_{k}"])), (name, k)
+
+
+def test_edge_rays(ctx, uploaded):
+    """Axis-aligned, zero, NaN and huge components, origins outside the box:
+    no fault, same answers as the oracle."""
+    sid, ref, box = uploaded["sphere5"]
+    o = np.array([[2.78, 2.78, -1.0], [-10, 2, -2], [2.78, 2.78, 0.0], [np.nan, 1, 1], [1, 1, 1], [2, 2, -2],
+                  [1e30, 0, 0], [2.78, 1.65, -3.5]], np.float32).T
+    d = np.array([[0, 0, -1], [1, 0, 0], [0, 0, 0], [1, 0, 0], [np.nan, 1, 0], [0, -1e-30, 0], [-1, 0, 0],
+                  [0, 1, 0]], np.float32).T
+    gpu = ctx.intersect(sid, o, d)
+    cpu = ref.intersect(o, d)
+    assert np.array_equal(gpu[0], cpu[0])
+
+
+def test_device_buffers(ctx, uploaded):
+    torch = pytest.importorskip("torch")
+    sid, ref, box = uploaded["sphere5"]
+    o, d = tg.make_rays(65_536, box, seed=5)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (*o, *d)]
+    out_i = torch.empty(o.shape[1], dtype=torch.int32, device="cuda")
+    outs = [torch.empty(o.shape[1], dtype=torch.float32, device="cuda") for _ in range(3)]
+    ctx.intersect_device(sid, [t.data_ptr() for t in dev], o.shape[1], [out_i.data_ptr()] + [t.data_ptr() for t in outs])
+    hid = out_i.cpu().numpy().view(np.uint32)
+    rid, rr, rs, rt = ref.intersect(o, d)
+    assert np.array_equal(hid, rid)
+    assert np.array_equal(bits(outs[0].cpu().numpy()), bits(rr))
+
+
+def test_empty_batch(ctx, uploaded):
+    sid = uploaded["room"][0]
+    z = np.zeros((3, 0), np.float32)
+    hid, r, s, t = ctx.intersect(sid, z, z)
+    assert hid.size == 0
+
+
+def test_bad_scene_rejected(ctx):
+    t = tg.KDTree.from_mesh(tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=2))
+    nodes, tris, box = t.export()
+    bad = nodes.copy()
+    inner = np.nonzero((nodes & np.uint64(3)) != np.uint64(3))[0][0]
+    bad[inner] = (bad[inner] & np.uint64(0xFFFFFFFF00000003)) | np.uint64((nodes.size + 3) << 2)
+    with pytest.raises(tg.TurnerError) as e:
+        ctx.upload(bad, tris, box)
+    assert e.value.status == tg.ERR_BAD_SCENE
+    with pytest.raises(tg.TurnerError):
+        ctx.intersect(999, np.zeros((3, 1), np.float32), np.ones((3, 1), np.float32))
+
+
+@pytest.mark.slow
+def test_full_hit_test_set(ctx):
+    """16,777,216 rays (origins uniform in the room, directions uniform on the
+    sphere) against the 327,692-triangle tree: every hit index equal."""
+    m = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=7, aspect=16 / 9)
+    t = tg.KDTree.from_mesh(m)
+    nodes, tris, box = t.export()
+    sid = ctx.upload(nodes, tris, box)
+    ref = orc.Scene(nodes, tris, box)
+    n = 1 << 24
+    o, d = tg.make_rays(n, box, seed=2024)
+    gpu = ctx.intersect(sid, o, d)
+    cpu = ref.intersect(o, d)
+    assert_same(gpu, cpu)
+    fast = ctx.intersect(sid, o, d, mode=tg.TRAVERSAL_FAST)
+    assert np.array_equal(fast[0], cpu[0])

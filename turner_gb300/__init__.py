@@ -1,0 +1,370 @@
+"""Python mirror of the GB300 path-tracing core's C ABI (include/turner_gpu.h).
+
+The native library turner_gb300/lib/libturner_gb300.so is the product; this
+module only binds it with ctypes. There is no Python or CPU fallback: if the
+library is missing or the GPU is not an sm_103 device, calls raise.
+
+Names follow the reference (turner-renderer/turner): a `KDTree` is built from
+triangles and uploaded as a scene; `Context.intersect` is the batched
+`KDTreeIntersection::intersect` (lib/kdtree.cpp:516-607); `Context.render` is
+the `pathtracer` render loop (main.cpp:181-236 around pathtracer.cpp:14-102).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+LIB_PATH = LIB_DIR / "libturner_gb300.so"
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_CUDA = -2
+ERR_OUT_OF_MEMORY = -3
+ERR_BAD_SCENE = -4
+ERR_TIMEOUT = -5
+ERR_DEVICE_BOUNDS = -6
+ERR_UNSUPPORTED = -7
+ERR_NO_DEVICE = -8
+ERR_TOO_LARGE = -9
+
+MISS = 0x40000000
+HOST_BUFFERS = 0
+DEVICE_BUFFERS = 1
+TRAVERSAL_PARITY = 0
+TRAVERSAL_FAST = 1
+SAMPLING_UNIFORM = 0
+SAMPLING_COSINE = 1
+
+SCENE_ROOM = 0
+SCENE_SPHERE_ROOM = 1
+SCENE_SOUP = 2
+SCENE_BAFFLE_ROOM = 3
+SCENE_BAFFLE_SPHERE = 4
+
+TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
+
+KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect")
+KERNEL_KINDS = len(KERNEL_NAMES)
+
+
+class TurnerError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = _lib().turner_strerror(status).decode() if _LIB is not None else str(status)
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("trafo", C.c_float * 9), ("delta_x", C.c_float),
+                ("aspect", C.c_float)]
+
+
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("color", C.c_float * 4)]
+
+
+class Job(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pixel_samples", C.c_uint32), ("max_depth", C.c_int32), ("monte_carlo_samples", C.c_int32),
+                ("exposure", C.c_float), ("inverse_gamma", C.c_float), ("gamma_correction", C.c_int32),
+                ("background", C.c_float * 3), ("seed", C.c_uint64), ("n_lights", C.c_int32),
+                ("light", Light), ("camera", Camera), ("sampling", C.c_int32), ("traversal", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("primary_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("device_ms", C.c_double)]
+
+
+_LIB = None
+_P = C.c_void_p
+
+
+def _lib() -> C.CDLL:
+    """Loads the native library; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(LIB_PATH))
+    sig = {
+        "turner_strerror": (C.c_char_p, [C.c_int]),
+        "turner_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+        "turner_destroy": (None, [_P]),
+        "turner_last_device_error": (C.c_int, [_P]),
+        "turner_last_error_message": (C.c_char_p, [_P]),
+        "turner_launch_count": (C.c_uint64, [_P]),
+        "turner_set_chunk_paths": (C.c_int, [_P, C.c_uint32]),
+        "turner_set_profiling": (C.c_int, [_P, C.c_int]),
+        "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
+        "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
+        "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
+        "turner_validate_nodes": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]),
+        "turner_intersect": (C.c_int, [_P, C.c_uint32] + [_P] * 6 + [C.c_uint64] + [_P] * 4 + [C.c_int, C.c_uint32]),
+        "turner_render": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.POINTER(_P), C.POINTER(Stats), C.c_uint32]),
+        "turner_render_accumulate": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, _P, C.POINTER(C.c_uint64),
+                                               C.c_uint32]),
+        "turner_kdtree_build": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, C.POINTER(_P)]),
+        "turner_kdtree_num_nodes": (C.c_uint32, [_P]),
+        "turner_kdtree_num_triangles": (C.c_uint32, [_P]),
+        "turner_kdtree_height": (C.c_uint32, [_P]),
+        "turner_kdtree_export": (C.c_int, [_P, _P, _P, _P]),
+        "turner_upload_kdtree": (C.c_int, [_P, _P, C.POINTER(C.c_uint32)]),
+        "turner_kdtree_free": (None, [_P]),
+        "turner_scene_make": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.POINTER(_P)]),
+        "turner_mesh_num_triangles": (C.c_uint32, [_P]),
+        "turner_mesh_vertices": (C.POINTER(C.c_float), [_P]),
+        "turner_mesh_normals": (C.POINTER(C.c_float), [_P]),
+        "turner_mesh_diffuse": (C.POINTER(C.c_float), [_P]),
+        "turner_mesh_camera": (None, [_P, C.POINTER(Camera), C.POINTER(C.c_float)]),
+        "turner_mesh_light": (C.c_int, [_P, C.POINTER(Light)]),
+        "turner_mesh_free": (None, [_P]),
+        "turner_make_rays": (C.c_int, [C.c_uint64, _P, C.c_uint64] + [_P] * 6),
+        "turner_write_p3": (C.c_uint64, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != OK:
+        raise TurnerError(status, what)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ------------------------------------------------------------------ scenes
+@dataclass
+class Mesh:
+    """Triangles of a synthetic scene plus its camera and light."""
+    vertices: np.ndarray  # (n, 9) float32
+    normals: np.ndarray   # (n, 9) float32
+    diffuse: np.ndarray   # (n, 4) float32
+    camera: Camera
+    hfov: float
+    light: Light | None
+
+    @property
+    def n_triangles(self) -> int:
+        return self.vertices.shape[0]
+
+
+def make_scene(kind: int, detail: int = 0, count: int = 0, seed: int = 1, aspect: float = 1.0) -> Mesh:
+    lib = _lib()
+    h = _P()
+    _check(lib.turner_scene_make(kind, detail, count, seed, aspect, C.byref(h)), "turner_scene_make")
+    try:
+        n = lib.turner_mesh_num_triangles(h)
+        v = np.ctypeslib.as_array(lib.turner_mesh_vertices(h), (n, 9)).copy()
+        nr = np.ctypeslib.as_array(lib.turner_mesh_normals(h), (n, 9)).copy()
+        d = np.ctypeslib.as_array(lib.turner_mesh_diffuse(h), (n, 4)).copy()
+        cam = Camera()
+        hfov = C.c_float()
+        lib.turner_mesh_camera(h, C.byref(cam), C.byref(hfov))
+        light = Light()
+        nl = lib.turner_mesh_light(h, C.byref(light))
+    finally:
+        lib.turner_mesh_free(h)
+    return Mesh(v, nr, d, cam, hfov.value, light if nl else None)
+
+
+def make_rays(n: int, box, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """Hit-test rays: origins uniform in `box`, directions uniform on S^2."""
+    o = np.empty((3, n), np.float32)
+    d = np.empty((3, n), np.float32)
+    b = np.asarray(box, np.float32)
+    _check(_lib().turner_make_rays(n, _ptr(b), seed, _ptr(o[0]), _ptr(o[1]), _ptr(o[2]), _ptr(d[0]), _ptr(d[1]),
+                                   _ptr(d[2])), "turner_make_rays")
+    return o, d
+
+
+class KDTree:
+    """KDTree::KDTree(Triangles) (lib/kdtree.cpp:474-490) on host threads."""
+
+    def __init__(self, vertices: np.ndarray, normals: np.ndarray | None = None, diffuse: np.ndarray | None = None,
+                 threads: int = 0):
+        lib = _lib()
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+        nr = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+        d = None if diffuse is None else np.ascontiguousarray(diffuse, np.float32).reshape(-1, 4)
+        self._h = _P()
+        _check(lib.turner_kdtree_build(_ptr(v), None if nr is None else _ptr(nr), None if d is None else _ptr(d),
+                                       v.shape[0], threads, C.byref(self._h)), "turner_kdtree_build")
+
+    @classmethod
+    def from_mesh(cls, mesh: Mesh, threads: int = 0) -> "KDTree":
+        return cls(mesh.vertices, mesh.normals, mesh.diffuse, threads)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.turner_kdtree_free(self._h)
+            self._h = None
+
+    def height(self) -> int:
+        return _lib().turner_kdtree_height(self._h)
+
+    def num_nodes(self) -> int:
+        return _lib().turner_kdtree_num_nodes(self._h)
+
+    def num_triangles(self) -> int:
+        return _lib().turner_kdtree_num_triangles(self._h)
+
+    def export(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(nodes uint64[n_nodes], triangles float32[n_tris, 48], box float32[6])."""
+        nodes = np.empty(self.num_nodes(), np.uint64)
+        tris = np.empty((self.num_triangles(), TRIANGLE_FLOATS), np.float32)
+        box = np.empty(6, np.float32)
+        _check(_lib().turner_kdtree_export(self._h, _ptr(nodes), _ptr(tris), _ptr(box)), "turner_kdtree_export")
+        return nodes, tris, box
+
+
+def validate_nodes(nodes: np.ndarray, n_tris: int) -> tuple[int, int]:
+    """(status, stack depth) of the host-side node-array check."""
+    n = np.ascontiguousarray(nodes, np.uint64)
+    depth = C.c_uint32(0)
+    st = _lib().turner_validate_nodes(_ptr(n), n.size, n_tris, C.byref(depth))
+    return st, depth.value
+
+
+# ---------------------------------------------------------------- context
+class Context:
+    """One GPU, one stream, the scenes uploaded to it."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib()
+        self._h = _P()
+        _check(lib.turner_create(C.byref(self._h), device), "turner_create")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.turner_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def launch_count(self) -> int:
+        return _lib().turner_launch_count(self._h)
+
+    def set_chunk_paths(self, paths: int) -> None:
+        _check(_lib().turner_set_chunk_paths(self._h, paths), "turner_set_chunk_paths")
+
+    def set_profiling(self, on: bool) -> None:
+        _check(_lib().turner_set_profiling(self._h, 1 if on else 0), "turner_set_profiling")
+
+    def kernel_times(self, reset: bool = False) -> dict:
+        """{kind: (milliseconds, launches)} measured with CUDA events."""
+        ms = np.zeros(KERNEL_KINDS, np.float64)
+        n = np.zeros(KERNEL_KINDS, np.uint64)
+        _check(_lib().turner_kernel_times(self._h, _ptr(ms), _ptr(n), 1 if reset else 0), "turner_kernel_times")
+        return {name: (float(ms[k]), int(n[k])) for k, name in enumerate(KERNEL_NAMES)}
+
+    def upload(self, nodes: np.ndarray, tris: np.ndarray, box: np.ndarray) -> int:
+        n = np.ascontiguousarray(nodes, np.uint64)
+        t = np.ascontiguousarray(tris, np.float32).reshape(-1, TRIANGLE_FLOATS)
+        b = np.ascontiguousarray(box, np.float32)
+        sid = C.c_uint32()
+        _check(_lib().turner_upload_scene(self._h, _ptr(n), n.size, _ptr(t), t.shape[0], _ptr(b), C.byref(sid)),
+               "turner_upload_scene")
+        return sid.value
+
+    def upload_tree(self, tree: KDTree) -> int:
+        sid = C.c_uint32()
+        _check(_lib().turner_upload_kdtree(self._h, tree._h, C.byref(sid)), "turner_upload_kdtree")
+        return sid.value
+
+    def free_scene(self, scene_id: int) -> None:
+        _check(_lib().turner_free_scene(self._h, scene_id), "turner_free_scene")
+
+    def intersect(self, scene_id: int, o: np.ndarray, d: np.ndarray, mode: int = TRAVERSAL_PARITY):
+        """Host-buffer batch intersect. o, d: (3, n) float32. Returns id, r, s, t."""
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = o.shape[1]
+        hid = np.empty(n, np.uint32)
+        r = np.empty(n, np.float32)
+        s = np.empty(n, np.float32)
+        t = np.empty(n, np.float32)
+        _check(_lib().turner_intersect(self._h, scene_id, _ptr(o[0]), _ptr(o[1]), _ptr(o[2]), _ptr(d[0]), _ptr(d[1]),
+                                       _ptr(d[2]), n, _ptr(hid), _ptr(r), _ptr(s), _ptr(t), mode, HOST_BUFFERS),
+               "turner_intersect")
+        return hid, r, s, t
+
+    def intersect_device(self, scene_id: int, ptrs: list[int], n: int, out_ptrs: list[int],
+                         mode: int = TRAVERSAL_PARITY) -> None:
+        """Device-buffer batch intersect (six ray pointers, four output pointers)."""
+        _check(_lib().turner_intersect(self._h, scene_id, *ptrs, n, *out_ptrs, mode, DEVICE_BUFFERS),
+               "turner_intersect")
+
+    def render(self, jobs: list[Job], outs: list[int] | None = None, flags: int = HOST_BUFFERS):
+        """Renders jobs; returns (images, stats). With flags=DEVICE_BUFFERS,
+        `outs` are device pointers and images is None."""
+        arr = (Job * len(jobs))(*jobs)
+        stats = (Stats * len(jobs))()
+        images = None
+        if flags == HOST_BUFFERS:
+            images = [np.empty((j.height, j.width, 4), np.float32) for j in jobs]
+            outs = [_ptr(im) for im in images]
+        ptrs = (_P * len(jobs))(*outs)
+        _check(_lib().turner_render(self._h, arr, len(jobs), ptrs, stats, flags), "turner_render")
+        return images, list(stats)
+
+
+def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, pixel_samples: int = 1,
+             max_depth: int = 3, monte_carlo_samples: int = 1, seed: int = 1, exposure: float = 1.0,
+             inverse_gamma: float = 0.454545, gamma_correction: bool = True, background=(0.0, 0.0, 0.0),
+             sampling: int = SAMPLING_UNIFORM, traversal: int = TRAVERSAL_PARITY) -> Job:
+    """A job with the reference's defaults (config.h, pathtracer.h)."""
+    j = Job()
+    j.scene_id = scene_id
+    j.width = width
+    j.height = height if height is not None else int(np.float32(width) / np.float32(mesh.camera.aspect))
+    j.pixel_samples = pixel_samples
+    j.max_depth = max_depth
+    j.monte_carlo_samples = monte_carlo_samples
+    j.exposure = exposure
+    j.inverse_gamma = np.float32(inverse_gamma)
+    j.gamma_correction = 1 if gamma_correction else 0
+    for k in range(3):
+        j.background[k] = background[k]
+    j.seed = seed
+    j.n_lights = 1 if mesh.light is not None else 0
+    if mesh.light is not None:
+        j.light = mesh.light
+    j.camera = mesh.camera
+    j.sampling = sampling
+    j.traversal = traversal
+    return j
+
+
+def write_p3(rgba: np.ndarray) -> str:
+    """P3 text of an (h, w, 4) float32 image (lib/raster.h:79-100)."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    h, w = a.shape[:2]
+    lib = _lib()
+    n = lib.turner_write_p3(_ptr(a), w, h, None, 0)
+    buf = C.create_string_buffer(n)
+    lib.turner_write_p3(_ptr(a), w, h, buf, n)
+    return buf.raw[:n].decode()

@@ -1,0 +1,540 @@
+// C ABI of the GB300 path-tracing core: contexts, scene upload with
+// validation, batched intersection and the wavefront render loop.
+#include "kernels.h"
+#include "turner_gpu.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+
+using namespace turner;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    // grows, never shrinks; contents are not preserved
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct SceneStore {
+    bool live = false;
+    DevBuf nodes, tri, shade;
+    SceneView view{};
+};
+
+int map_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return TURNER_OK;
+    if (e == cudaErrorMemoryAllocation) return TURNER_ERR_OUT_OF_MEMORY;
+    return TURNER_ERR_CUDA;
+}
+
+} // namespace
+
+struct turner_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<std::unique_ptr<SceneStore>> scenes;
+    // render workspace
+    DevBuf L, qa[4], qb[4], hits, shq[3], counters, image, rays_in, rays_out;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
+    uint64_t launches = 0;
+    std::string last_error;
+    // optional per-kernel timing: event pairs around launches, summed per kind
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, size_t>> ev_used;   // (kernel kind, first event index)
+    double kernel_ms[TURNER_KERNEL_KINDS] = {};
+    uint64_t kernel_launches[TURNER_KERNEL_KINDS] = {};
+};
+
+#define TURNER_CK(call)                                                                      \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            ctx->last_error = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+            return map_cuda(e_);                                                             \
+        }                                                                                    \
+    } while (0)
+
+namespace {
+
+// Brackets one kernel launch with an event pair when profiling is on.
+struct KernelTimer {
+    turner_ctx* ctx;
+    int kind;
+    size_t first = 0;
+    bool on = false;
+    KernelTimer(turner_ctx* c, int k) : ctx(c), kind(k) {
+        ctx->launches += 1;
+        if (!ctx->profiling) return;
+        first = ctx->ev_used.size() * 2;
+        while (ctx->ev_pool.size() < first + 2) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            ctx->ev_pool.push_back(e);
+        }
+        cudaEventRecord(ctx->ev_pool[first], ctx->stream);
+        on = true;
+    }
+    ~KernelTimer() {
+        if (!on) return;
+        cudaEventRecord(ctx->ev_pool[first + 1], ctx->stream);
+        ctx->ev_used.emplace_back(kind, first);
+    }
+};
+
+// After a stream synchronize: folds the recorded event pairs into the totals.
+void collect_kernel_times(turner_ctx* ctx) {
+    for (const auto& u : ctx->ev_used) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ctx->ev_pool[u.second], ctx->ev_pool[u.second + 1]) == cudaSuccess) {
+            ctx->kernel_ms[u.first] += ms;
+            ctx->kernel_launches[u.first] += 1;
+        }
+    }
+    ctx->ev_used.clear();
+}
+
+// Walks the tree from the root as the traversal does and checks that it stays
+// inside the arrays: child indices point forward and in range, leaf ids are
+// valid triangles, every leaf run ends (half-empty leaf or inner node) before
+// the end of the array. Returns the stack depth traversal needs (the largest
+// number of inner nodes on a root-to-leaf path), or -1.
+long validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris) {
+    if (n_nodes == 0) return -1;
+    std::vector<uint32_t> order;        // reachable inner nodes, discovery order
+    std::vector<uint8_t> seen(n_nodes, 0);
+    std::vector<uint32_t> st{0};
+    seen[0] = 1;
+    while (!st.empty()) {
+        const uint32_t i = st.back();
+        st.pop_back();
+        const uint64_t w = nodes[i];
+        const uint32_t lo = static_cast<uint32_t>(w);
+        if ((lo & 3u) != 3u) {
+            const uint32_t right = lo >> 2;
+            if (i + 1 >= n_nodes || right <= i || right >= n_nodes) return -1;
+            order.push_back(i);
+            for (uint32_t c : {i + 1, right}) {
+                if (!seen[c]) {
+                    seen[c] = 1;
+                    st.push_back(c);
+                }
+            }
+        } else {
+            for (uint32_t j = i;;) {
+                const uint64_t lw = nodes[j];
+                const uint32_t l = static_cast<uint32_t>(lw);
+                if (static_cast<uint32_t>(lw >> 32) >= n_tris) return -1;
+                if (l == 0xFFFFFFFFu) break;
+                if ((l >> 2) >= n_tris) return -1;
+                if (++j >= n_nodes) return -1;
+                if ((static_cast<uint32_t>(nodes[j]) & 3u) != 3u) break;
+            }
+        }
+    }
+    // depth by decreasing index: children have larger indices than parents
+    std::vector<uint16_t> h(n_nodes, 0);
+    std::sort(order.begin(), order.end());
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const uint32_t i = *it;
+        const uint32_t right = static_cast<uint32_t>(nodes[i]) >> 2;
+        const uint32_t hl = seen[i + 1] ? h[i + 1] : 0, hr = seen[right] ? h[right] : 0;
+        h[i] = static_cast<uint16_t>(std::min<uint32_t>(60000, 1 + std::max(hl, hr)));
+    }
+    return h[0];
+}
+
+void fill_job(const turner_job& j, const SceneView& sc, JobDev& d) {
+    std::memset(&d, 0, sizeof(d));
+    d.sc = sc;
+    std::memcpy(d.cam_pos, j.camera.position, sizeof(d.cam_pos));
+    std::memcpy(d.trafo, j.camera.trafo, sizeof(d.trafo));
+    d.delta_x = j.camera.delta_x;
+    d.delta_y = j.camera.delta_x / j.camera.aspect;   // lib/types.h:104
+    d.width = j.width;
+    d.height = j.height;
+    d.spp = j.pixel_samples;
+    d.max_depth = j.max_depth;
+    d.mc = j.monte_carlo_samples;
+    std::memcpy(d.bg, j.background, sizeof(d.bg));
+    d.seed = j.seed;
+    d.n_lights = j.n_lights;
+    std::memcpy(d.light_pos, j.light.position, sizeof(d.light_pos));
+    std::memcpy(d.light_col, j.light.color, sizeof(d.light_col));
+    d.sampling = j.sampling;
+    d.traversal = j.traversal;
+    d.exposure = j.exposure;
+    d.inv_gamma = j.inverse_gamma;
+    d.gamma = j.gamma_correction;
+    d.tone_map = 1;
+}
+
+int check_job(turner_ctx* ctx, const turner_job& j) {
+    if (j.scene_id >= ctx->scenes.size() || !ctx->scenes[j.scene_id]->live) return TURNER_ERR_INVALID_ARG;
+    if (j.width == 0 || j.height == 0 || j.pixel_samples == 0 || j.max_depth < 0) return TURNER_ERR_INVALID_ARG;
+    if (!(j.camera.aspect > 0)) return TURNER_ERR_INVALID_ARG;
+    if (j.monte_carlo_samples < 0 || j.n_lights < 0 || j.n_lights > 1) return TURNER_ERR_INVALID_ARG;
+    if (j.monte_carlo_samples > 1) return TURNER_ERR_UNSUPPORTED;
+    if (j.sampling != TURNER_SAMPLING_UNIFORM && j.sampling != TURNER_SAMPLING_COSINE) return TURNER_ERR_INVALID_ARG;
+    if (j.traversal != TURNER_TRAVERSAL_PARITY && j.traversal != TURNER_TRAVERSAL_FAST) return TURNER_ERR_INVALID_ARG;
+    if (uint64_t(j.width) * j.height > (1ull << 31)) return TURNER_ERR_TOO_LARGE;
+    if (j.max_depth > 64) return TURNER_ERR_TOO_LARGE;
+    return TURNER_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* turner_strerror(int status) {
+    switch (status) {
+    case TURNER_OK: return "ok";
+    case TURNER_ERR_INVALID_ARG: return "invalid argument";
+    case TURNER_ERR_CUDA: return "CUDA runtime error";
+    case TURNER_ERR_OUT_OF_MEMORY: return "out of memory";
+    case TURNER_ERR_BAD_SCENE: return "node array failed validation";
+    case TURNER_ERR_TIMEOUT: return "bounded device wait timed out";
+    case TURNER_ERR_DEVICE_BOUNDS: return "device-side index check failed";
+    case TURNER_ERR_UNSUPPORTED: return "unsupported parameter combination";
+    case TURNER_ERR_NO_DEVICE: return "no suitable CUDA device";
+    case TURNER_ERR_TOO_LARGE: return "request exceeds a documented maximum";
+    default: return "unknown status";
+    }
+}
+
+int turner_create(turner_ctx** out, int device) {
+    if (!out) return TURNER_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return TURNER_ERR_NO_DEVICE;
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return TURNER_ERR_NO_DEVICE;
+    if (prop.major * 10 + prop.minor != 103) return TURNER_ERR_NO_DEVICE;   // built for sm_103a only
+    auto* ctx = new (std::nothrow) turner_ctx;
+    if (!ctx) return TURNER_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return map_cuda(e);
+    }
+    *out = ctx;
+    return TURNER_OK;
+}
+
+void turner_destroy(turner_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->scenes.clear();
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int turner_last_device_error(turner_ctx* ctx) { return ctx ? TURNER_OK : TURNER_ERR_INVALID_ARG; }
+
+uint64_t turner_launch_count(turner_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+const char* turner_last_error_message(turner_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int turner_validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t* stack_depth) {
+    if (!nodes || n_nodes == 0 || n_tris == 0) return TURNER_ERR_INVALID_ARG;
+    const long depth = validate_nodes(nodes, n_nodes, n_tris);
+    if (depth < 0) return TURNER_ERR_BAD_SCENE;
+    if (stack_depth) *stack_depth = static_cast<uint32_t>(depth);
+    return depth > kStackCap ? TURNER_ERR_TOO_LARGE : TURNER_OK;
+}
+
+int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes, const turner_triangle* tris,
+                        uint32_t n_tris, const float box[6], uint32_t* scene_id) {
+    if (!ctx || !nodes || !tris || !box || !scene_id || n_nodes == 0 || n_tris == 0) return TURNER_ERR_INVALID_ARG;
+    if (n_tris >= TURNER_MISS || n_nodes >= TURNER_MISS) return TURNER_ERR_TOO_LARGE;
+    const long depth = validate_nodes(nodes, n_nodes, n_tris);
+    if (depth < 0) return TURNER_ERR_BAD_SCENE;
+    if (depth > kStackCap) return TURNER_ERR_TOO_LARGE;
+    TURNER_CK(cudaSetDevice(ctx->device));
+
+    auto sc = std::unique_ptr<SceneStore>(new (std::nothrow) SceneStore);
+    if (!sc) return TURNER_ERR_OUT_OF_MEMORY;
+    std::vector<float4> tri(4 * size_t(n_tris)), shade(4 * size_t(n_tris));
+    for (uint32_t i = 0; i < n_tris; ++i) {
+        const turner_triangle& t = tris[i];
+        tri[4 * i + 0] = make_float4(t.vertices[0][0], t.vertices[0][1], t.vertices[0][2], t.uv);
+        tri[4 * i + 1] = make_float4(t.normal[0], t.normal[1], t.normal[2], t.vv);
+        tri[4 * i + 2] = make_float4(t.u[0], t.u[1], t.u[2], t.uu);
+        tri[4 * i + 3] = make_float4(t.v[0], t.v[1], t.v[2], t.denom);
+        shade[4 * i + 0] = make_float4(t.normals[0][0], t.normals[0][1], t.normals[0][2], t.diffuse[0]);
+        shade[4 * i + 1] = make_float4(t.normals[1][0], t.normals[1][1], t.normals[1][2], t.diffuse[1]);
+        shade[4 * i + 2] = make_float4(t.normals[2][0], t.normals[2][1], t.normals[2][2], t.diffuse[2]);
+        shade[4 * i + 3] = make_float4(t.diffuse[3], 0.f, 0.f, 0.f);
+    }
+    TURNER_CK(sc->nodes.ensure(sizeof(uint64_t) * n_nodes));
+    TURNER_CK(sc->tri.ensure(sizeof(float4) * tri.size()));
+    TURNER_CK(sc->shade.ensure(sizeof(float4) * shade.size()));
+    TURNER_CK(cudaMemcpyAsync(sc->nodes.p, nodes, sizeof(uint64_t) * n_nodes, cudaMemcpyHostToDevice, ctx->stream));
+    TURNER_CK(cudaMemcpyAsync(sc->tri.p, tri.data(), sizeof(float4) * tri.size(), cudaMemcpyHostToDevice, ctx->stream));
+    TURNER_CK(cudaMemcpyAsync(sc->shade.p, shade.data(), sizeof(float4) * shade.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    SceneView& v = sc->view;
+    v.nodes = sc->nodes.as<uint2>();
+    v.tri = sc->tri.as<float4>();
+    v.shade = sc->shade.as<float4>();
+    for (int k = 0; k < 3; ++k) {
+        v.lo[k] = box[k];
+        v.hi[k] = box[3 + k];
+    }
+    v.n_nodes = n_nodes;
+    v.n_tris = n_tris;
+    v.height = static_cast<uint32_t>(depth);
+    sc->live = true;
+    ctx->scenes.push_back(std::move(sc));
+    *scene_id = static_cast<uint32_t>(ctx->scenes.size() - 1);
+    return TURNER_OK;
+}
+
+int turner_free_scene(turner_ctx* ctx, uint32_t scene_id) {
+    if (!ctx || scene_id >= ctx->scenes.size() || !ctx->scenes[scene_id]->live) return TURNER_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    auto& sc = *ctx->scenes[scene_id];
+    sc.nodes.release();
+    sc.tri.release();
+    sc.shade.release();
+    sc.live = false;
+    return TURNER_OK;
+}
+
+int turner_upload_kdtree(turner_ctx* ctx, const turner_kdtree* tree, uint32_t* scene_id) {
+    if (!ctx || !tree) return TURNER_ERR_INVALID_ARG;
+    const uint32_t nn = turner_kdtree_num_nodes(tree), nt = turner_kdtree_num_triangles(tree);
+    std::vector<uint64_t> nodes(nn);
+    std::vector<turner_triangle> tris(nt);
+    float box[6];
+    int st = turner_kdtree_export(tree, nodes.data(), tris.data(), box);
+    if (st != TURNER_OK) return st;
+    return turner_upload_scene(ctx, nodes.data(), nn, tris.data(), nt, box, scene_id);
+}
+
+int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
+                     const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id, float* r,
+                     float* s, float* t, int mode, uint32_t flags) {
+    if (!ctx || scene_id >= ctx->scenes.size() || !ctx->scenes[scene_id]->live) return TURNER_ERR_INVALID_ARG;
+    if (!ox || !oy || !oz || !dx || !dy || !dz || !hit_id || !r || !s || !t) return TURNER_ERR_INVALID_ARG;
+    if (mode != TURNER_TRAVERSAL_PARITY && mode != TURNER_TRAVERSAL_FAST) return TURNER_ERR_INVALID_ARG;
+    if (flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
+    if (n == 0) return TURNER_OK;
+    TURNER_CK(cudaSetDevice(ctx->device));
+    const SceneView& sc = ctx->scenes[scene_id]->view;
+    const int fast = mode == TURNER_TRAVERSAL_FAST;
+    if (flags == TURNER_DEVICE_BUFFERS) {
+        {
+            KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);
+            launch_intersect(sc, ox, oy, oz, dx, dy, dz, n, hit_id, r, s, t, fast, ctx->stream);
+        }
+        TURNER_CK(cudaGetLastError());
+        TURNER_CK(cudaStreamSynchronize(ctx->stream));
+        collect_kernel_times(ctx);
+        return TURNER_OK;
+    }
+    // host buffers: stage through device memory in slices
+    const uint64_t slice = std::min<uint64_t>(n, 1ull << 24);
+    TURNER_CK(ctx->rays_in.ensure(6 * sizeof(float) * slice));
+    TURNER_CK(ctx->rays_out.ensure(4 * sizeof(float) * slice));
+    float* din = ctx->rays_in.as<float>();
+    float* dout = ctx->rays_out.as<float>();
+    const float* src[6] = {ox, oy, oz, dx, dy, dz};
+    for (uint64_t b = 0; b < n; b += slice) {
+        const uint64_t m = std::min(slice, n - b);
+        for (int k = 0; k < 6; ++k) {
+            TURNER_CK(cudaMemcpyAsync(din + k * slice, src[k] + b, m * sizeof(float), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        }
+        {
+            KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);
+            launch_intersect(sc, din, din + slice, din + 2 * slice, din + 3 * slice, din + 4 * slice,
+                             din + 5 * slice, m, reinterpret_cast<uint32_t*>(dout), dout + slice, dout + 2 * slice,
+                             dout + 3 * slice, fast, ctx->stream);
+        }
+        TURNER_CK(cudaGetLastError());
+        TURNER_CK(cudaMemcpyAsync(hit_id + b, dout, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        TURNER_CK(cudaMemcpyAsync(r + b, dout + slice, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        TURNER_CK(cudaMemcpyAsync(s + b, dout + 2 * slice, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        TURNER_CK(cudaMemcpyAsync(t + b, dout + 3 * slice, m * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    collect_kernel_times(ctx);
+    return TURNER_OK;
+}
+
+int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths) {
+    if (!ctx || paths < 1024) return TURNER_ERR_INVALID_ARG;
+    ctx->chunk_paths = paths;
+    return TURNER_OK;
+}
+
+int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float* const* out_rgba,
+                  turner_stats* stats, uint32_t flags) {
+    if (!ctx || !jobs || !out_rgba || n_jobs == 0 || flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        if (!out_rgba[j]) return TURNER_ERR_INVALID_ARG;
+        const int st = check_job(ctx, jobs[j]);
+        if (st != TURNER_OK) return st;
+    }
+    TURNER_CK(cudaSetDevice(ctx->device));
+
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const turner_job& job = jobs[j];
+        JobDev jd;
+        fill_job(job, ctx->scenes[job.scene_id]->view, jd);
+        const uint64_t n_pixels = uint64_t(job.width) * job.height;
+        const uint32_t px_per_chunk =
+            static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(n_pixels, ctx->chunk_paths / job.pixel_samples)));
+        const uint32_t cap = px_per_chunk * job.pixel_samples;
+        const int levels = job.max_depth + 1;
+
+        TURNER_CK(ctx->L.ensure(sizeof(float4) * cap));
+        for (int k = 0; k < 3; ++k) {
+            TURNER_CK(ctx->qa[k].ensure(sizeof(float4) * cap));
+            TURNER_CK(ctx->qb[k].ensure(sizeof(float4) * cap));
+            TURNER_CK(ctx->shq[k].ensure(sizeof(float4) * cap));
+        }
+        TURNER_CK(ctx->qa[3].ensure(sizeof(uint2) * cap));
+        TURNER_CK(ctx->qb[3].ensure(sizeof(uint2) * cap));
+        TURNER_CK(ctx->hits.ensure(sizeof(Hit) * cap));
+        const uint64_t n_chunks = (n_pixels + px_per_chunk - 1) / px_per_chunk;
+        TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * 2 * (levels + 1) * n_chunks));
+        float4* image = reinterpret_cast<float4*>(out_rgba[j]);
+        if (flags == TURNER_HOST_BUFFERS) {
+            TURNER_CK(ctx->image.ensure(sizeof(float4) * n_pixels));
+            image = ctx->image.as<float4>();
+        }
+        uint32_t* counters = ctx->counters.as<uint32_t>();
+        TURNER_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * 2 * (levels + 1) * n_chunks, ctx->stream));
+        TURNER_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+
+        RayQueue qa{ctx->qa[0].as<float4>(), ctx->qa[1].as<float4>(), ctx->qa[2].as<float4>(), ctx->qa[3].as<uint2>(),
+                    nullptr};
+        RayQueue qb{ctx->qb[0].as<float4>(), ctx->qb[1].as<float4>(), ctx->qb[2].as<float4>(), ctx->qb[3].as<uint2>(),
+                    nullptr};
+        ShadowQueue sh{ctx->shq[0].as<float4>(), ctx->shq[1].as<float4>(), ctx->shq[2].as<float4>(), nullptr};
+        for (uint64_t c = 0; c < n_chunks; ++c) {
+            const uint32_t first = static_cast<uint32_t>(c * px_per_chunk);
+            const uint32_t npx = static_cast<uint32_t>(std::min<uint64_t>(px_per_chunk, n_pixels - first));
+            const uint32_t n_paths = npx * job.pixel_samples;
+            uint32_t* cnt = counters + 2 * (levels + 1) * c;   // [ray counts per level | shadow counts per level]
+            RayQueue cur = qa, nxt = qb;
+            cur.count = cnt;
+            {
+                KernelTimer kt(ctx, TURNER_KERNEL_CAMERA);
+                launch_camera(jd, first, n_paths, cur, ctx->L.as<float4>(), ctx->stream);
+            }
+            for (int depth = 0; depth <= job.max_depth; ++depth) {
+                nxt.count = cnt + depth + 1;
+                sh.count = cnt + (levels + 1) + depth;
+                {
+                    KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
+                    launch_trace(jd.sc, cur, ctx->hits.as<Hit>(), n_paths, job.traversal == TURNER_TRAVERSAL_FAST,
+                                 ctx->stream);
+                }
+                {
+                    KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
+                    launch_shade(jd, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), n_paths,
+                                 ctx->stream);
+                }
+                {
+                    KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
+                    launch_shadow(jd.sc, sh, ctx->L.as<float4>(), n_paths, ctx->stream);
+                }
+                std::swap(cur, nxt);
+            }
+            {
+                KernelTimer kt(ctx, TURNER_KERNEL_RESOLVE);
+                launch_resolve(jd, first, npx, ctx->L.as<float4>(), image, ctx->stream);
+            }
+            TURNER_CK(cudaGetLastError());
+        }
+        TURNER_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        if (flags == TURNER_HOST_BUFFERS) {
+            TURNER_CK(cudaMemcpyAsync(out_rgba[j], image, sizeof(float4) * n_pixels, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        }
+        std::vector<uint32_t> host_cnt(2 * (levels + 1) * n_chunks);
+        TURNER_CK(cudaMemcpyAsync(host_cnt.data(), counters, sizeof(uint32_t) * host_cnt.size(),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+        TURNER_CK(cudaStreamSynchronize(ctx->stream));
+        collect_kernel_times(ctx);
+        if (stats) {
+            turner_stats& st = stats[j];
+            st.rays = st.primary_rays = st.shadow_rays = 0;
+            for (uint64_t c = 0; c < n_chunks; ++c) {
+                const uint32_t* cc = host_cnt.data() + 2 * (levels + 1) * c;
+                st.primary_rays += cc[0];
+                for (int k = 0; k < levels; ++k) {
+                    st.rays += cc[k];
+                    st.shadow_rays += cc[levels + 1 + k];
+                }
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+            st.device_ms = ms;
+        }
+    }
+    return TURNER_OK;
+}
+
+int turner_set_profiling(turner_ctx* ctx, int on) {
+    if (!ctx) return TURNER_ERR_INVALID_ARG;
+    ctx->profiling = on != 0;
+    return TURNER_OK;
+}
+
+int turner_kernel_times(turner_ctx* ctx, double* ms, uint64_t* launches, int reset) {
+    if (!ctx) return TURNER_ERR_INVALID_ARG;
+    for (int k = 0; k < TURNER_KERNEL_KINDS; ++k) {
+        if (ms) ms[k] = ctx->kernel_ms[k];
+        if (launches) launches[k] = ctx->kernel_launches[k];
+        if (reset) {
+            ctx->kernel_ms[k] = 0;
+            ctx->kernel_launches[k] = 0;
+        }
+    }
+    return TURNER_OK;
+}
+
+int turner_render_accumulate(turner_ctx*, const turner_job*, uint32_t, double*, uint64_t*, uint32_t) {
+    return TURNER_ERR_UNSUPPORTED;
+}
+
+} // extern "C"

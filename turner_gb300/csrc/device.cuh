@@ -1,0 +1,231 @@
+// Device-side scene layout, geometry and kd-tree traversal.
+//
+// The translation units that include this header are compiled with
+// -fmad=false (and IEEE division / square root, the nvcc defaults), so every
+// expression below rounds exactly like the reference's C++ built with
+// -ffp-contract=off: hit indices are bit-identical to the reference's
+// KDTreeIntersection::intersect, not merely close.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace turner {
+
+constexpr uint32_t kMiss = 0x40000000u;     // FlatNode::MAX_TRIANGLE_ID (lib/kdtree.h:66)
+constexpr float kEps = 0.00001f;            // lib/types.h:14
+constexpr float kFltMax = 3.40282346638528859812e+38f;
+constexpr int kStackCap = 128;              // entries; scenes deeper than this are rejected
+
+// HBM layout of one uploaded scene.
+//   nodes : FlatNode words verbatim, read as uint2 {lo = type/axis/right or
+//           second id, hi = split bits or first id}; DFS order keeps the near
+//           child adjacent to its parent.
+//   tri   : 64-byte intersection record per triangle, 4 x float4:
+//           {v0, uv} {normal, vv} {u, uu} {v, denom}; the first two (one
+//           32-byte sector) decide the plane test, the rest is read only for
+//           the barycentric test.
+//   shade : 64-byte shading record per triangle, read once per hit:
+//           {n0, diffuse.r} {n1, diffuse.g} {n2, diffuse.b} {diffuse.a, 0, 0, 0}
+struct SceneView {
+    const uint2* nodes;
+    const float4* tri;
+    const float4* shade;
+    float lo[3], hi[3];
+    uint32_t n_nodes, n_tris, height;
+};
+
+struct Hit {
+    uint32_t id;
+    float r, s, t;
+};
+
+// intersect_ray_plane + intersect_ray_triangle (lib/intersection.h:40-89)
+__device__ __forceinline__ bool triangle_test(const float4* __restrict__ tri, uint32_t id, float3 o, float3 d, float& r,
+                                              float& s, float& t) {
+    const float4 a = __ldg(tri + 4 * size_t(id) + 0);   // v0, uv
+    const float4 n = __ldg(tri + 4 * size_t(id) + 1);   // normal, vv
+    const float denom = n.x * d.x + n.y * d.y + n.z * d.z;
+    if (denom == 0.f) return false;                      // r = lowest < 0
+    const float nom = n.x * (a.x - o.x) + n.y * (a.y - o.y) + n.z * (a.z - o.z);
+    r = nom / denom;
+    if (r < 0) return false;                             // NaN continues, as in the reference
+    const float4 u = __ldg(tri + 4 * size_t(id) + 2);   // u, uu
+    const float4 v = __ldg(tri + 4 * size_t(id) + 3);   // v, denom
+    const float wx = (o.x + r * d.x) - a.x;
+    const float wy = (o.y + r * d.y) - a.y;
+    const float wz = (o.z + r * d.z) - a.z;
+    const float wv = wx * v.x + wy * v.y + wz * v.z;
+    const float wu = wx * u.x + wy * u.y + wz * u.z;
+    s = (a.w * wv - n.w * wu) / v.w;
+    if (s < 0) return false;
+    t = (a.w * wu - u.w * wv) / v.w;
+    if (t < 0 || 1 < s + t) return false;
+    return true;
+}
+
+__device__ __forceinline__ float pick(float3 v, uint32_t ax) { return ax == 0 ? v.x : (ax == 1 ? v.y : v.z); }
+
+// KDTreeIntersection::intersect (lib/kdtree.cpp:516-607).
+//   CLOSEST: every leaf overlapped by [tenter, texit] is visited in the
+//   reference's order (near child first, far child pushed, LIFO), and the
+//   first strict minimum of r is kept. Keeping one running minimum with a
+//   strict "<" picks the same triangle as the reference's per-run minimum
+//   followed by a strict comparison with the best so far.
+//   ANY (shadow rays): returns a hit as soon as one valid intersection has
+//   r <= tmax. The reference tests `!hit || r_closest > dist`; "lit" is the
+//   same predicate as "no valid intersection with r <= dist", so this is exact.
+//   FAST_EXIT (closest only): after a leaf run, stop when the best r is below
+//   every pending cell's entry distance minus a margin.
+template <bool ANY, bool FAST_EXIT>
+__device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d, float tmax) {
+    Hit best{kMiss, kFltMax, 0.f, 0.f};
+    // fix_direction (kdtree.cpp:503-511)
+    const float3 fd = make_float3(d.x == 0.f ? kEps : d.x, d.y == 0.f ? kEps : d.y, d.z == 0.f ? kEps : d.z);
+    const float3 inv = make_float3(1.0f / fd.x, 1.0f / fd.y, 1.0f / fd.z);
+    // intersect_ray_box (intersection.h:105-128) on the fixed ray
+    float tenter, texit;
+    {
+        const float tx1 = (sc.lo[0] - o.x) * inv.x, tx2 = (sc.hi[0] - o.x) * inv.x;
+        tenter = fminf(tx1, tx2);
+        texit = fmaxf(tx1, tx2);
+        const float ty1 = (sc.lo[1] - o.y) * inv.y, ty2 = (sc.hi[1] - o.y) * inv.y;
+        tenter = fmaxf(tenter, fminf(ty1, ty2));
+        texit = fminf(texit, fmaxf(ty1, ty2));
+        const float tz1 = (sc.lo[2] - o.z) * inv.z, tz2 = (sc.hi[2] - o.z) * inv.z;
+        tenter = fmaxf(tenter, fminf(tz1, tz2));
+        texit = fminf(texit, fmaxf(tz1, tz2));
+        if (texit < tenter) return best;
+    }
+
+    uint32_t st_node[kStackCap];
+    float st_enter[kStackCap], st_exit[kStackCap];
+    int sp = 0;
+    uint32_t node = 0;
+    const uint2* __restrict__ nodes = sc.nodes;
+    for (;;) {
+        uint2 w = __ldg(nodes + node);
+        while ((w.x & 3u) != 3u) {
+            const uint32_t ax = w.x & 3u;
+            const float t = (__uint_as_float(w.y) - pick(o, ax)) * pick(inv, ax);
+            uint32_t near_c = node + 1, far_c = w.x >> 2;
+            if (pick(fd, ax) <= 0.f) {
+                const uint32_t tmp = near_c;
+                near_c = far_c;
+                far_c = tmp;
+            }
+            if (texit < t) {
+                node = near_c;
+            } else if (t < tenter) {
+                node = far_c;
+            } else {
+                st_node[sp] = far_c;
+                st_enter[sp] = t;
+                st_exit[sp] = texit;
+                ++sp;
+                node = near_c;
+                texit = t;
+            }
+            w = __ldg(nodes + node);
+        }
+        // leaf run: two ids per word until a half-empty leaf or an inner node
+        for (;;) {
+            float r, s, t;
+            if (triangle_test(sc.tri, w.y, o, d, r, s, t)) {
+                if (ANY) {
+                    if (r <= tmax) return Hit{w.y, r, s, t};
+                } else if (r < best.r) {
+                    best = Hit{w.y, r, s, t};
+                }
+            }
+            if (w.x == 0xFFFFFFFFu) break;
+            const uint32_t id2 = w.x >> 2;
+            if (triangle_test(sc.tri, id2, o, d, r, s, t)) {
+                if (ANY) {
+                    if (r <= tmax) return Hit{id2, r, s, t};
+                } else if (r < best.r) {
+                    best = Hit{id2, r, s, t};
+                }
+            }
+            ++node;
+            w = __ldg(nodes + node);
+            if ((w.x & 3u) != 3u) break;
+        }
+        if (sp == 0) break;
+        --sp;
+        if (FAST_EXIT && !ANY) {
+            // cells are popped in increasing entry distance along the ray;
+            // a hit closer than the next cell's entry (with margin for the
+            // thick-plane classification of the builder) cannot be beaten
+            if (best.r < st_enter[sp] - (1e-3f + 1e-3f * fabsf(st_enter[sp]))) break;
+        }
+        node = st_node[sp];
+        tenter = st_enter[sp];
+        texit = st_exit[sp];
+    }
+    return best;
+}
+
+// xorshift64* (lib/xorshift.h:27-70): float = (x & (2^24 - 1)) * 2^-24
+__device__ __forceinline__ float xorshift_float(uint64_t& s) {
+    s ^= s >> 12;
+    s ^= s << 25;
+    s ^= s >> 27;
+    const uint64_t x = s * 2685821657736338717ULL;
+    return static_cast<float>(static_cast<uint32_t>(x & 0xFFFFFFull)) * 5.9604644775390625e-8f;
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    uint64_t z = x + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// Per-(pixel, sample) streams: key = pixel_index * spp + sample.
+__device__ __forceinline__ void path_seeds(uint64_t seed, uint64_t key, uint64_t& jitter, uint64_t& bounce) {
+    const uint64_t a = splitmix64(seed ^ key);
+    const uint64_t b = splitmix64(a ^ 0xD1B54A32D192ED03ULL);
+    jitter = a ? a : 1;
+    bounce = b ? b : 1;
+}
+
+// Moeller-Hughes from-to rotation (JGT 1999) taking (0, 0, 1) onto n, row-major.
+__device__ __forceinline__ void from_to_z(float3 n, float m[9]) {
+    const float fx = 0.f, fy = 0.f, fz = 1.f;
+    const float vx = fy * n.z - fz * n.y;
+    const float vy = fz * n.x - fx * n.z;
+    const float vz = fx * n.y - fy * n.x;
+    const float e = fx * n.x + fy * n.y + fz * n.z;
+    const float f = e < 0 ? -e : e;
+    if (f > 1.0f - 0.000001f) {
+        // `from` = +z is least aligned with the y axis (|0| < |1|, ties -> y)
+        const float x0 = 0.f, x1 = 1.f, x2 = 0.f;
+        const float u[3] = {x0 - fx, x1 - fy, x2 - fz};
+        const float w[3] = {x0 - n.x, x1 - n.y, x2 - n.z};
+        const float c1 = 2.0f / (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        const float c2 = 2.0f / (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        const float c3 = c1 * c2 * (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) m[3 * i + j] = -c1 * u[i] * u[j] - c2 * w[i] * w[j] + c3 * w[i] * u[j];
+            m[3 * i + i] += 1.0f;
+        }
+    } else {
+        const float h = 1.0f / (1.0f + e);
+        const float hvx = h * vx, hvz = h * vz;
+        const float hvxy = hvx * vy, hvxz = hvx * vz, hvyz = hvz * vy;
+        m[0] = e + hvx * vx;
+        m[1] = hvxy - vz;
+        m[2] = hvxz + vy;
+        m[3] = hvxy + vz;
+        m[4] = e + h * vy * vy;
+        m[5] = hvyz - vx;
+        m[6] = hvxz - vy;
+        m[7] = hvyz + vx;
+        m[8] = e + hvz * vz;
+    }
+}
+
+} // namespace turner

@@ -272,14 +272,28 @@ void soup(Builder& b, uint32_t count, uint64_t seed) {
     Rng rng{splitmix64(seed ^ 0x5D1CEULL)};
     const D3 lo{0.5 * kRoom - 0.5, 1.2, -0.5 * kRoom - 0.5};
     std::vector<D3> centers(64);
-    for (auto& c : centers) c = lo + D3{rng.uniform(), rng.uniform(), rng.uniform()};
+    for (auto& c : centers) {
+        const double cx = rng.uniform();
+        const double cy = rng.uniform();
+        const double cz = rng.uniform();
+        c = lo + D3{cx, cy, cz};
+    }
     for (uint32_t i = 0; i < count; ++i) {
         const D3 c = centers[static_cast<size_t>(rng.uniform() * 64) & 63];
-        D3 v0 = c + D3{rng.range(-0.12, 0.12), rng.range(-0.12, 0.12), rng.range(-0.12, 0.12)};
+        const double ox = rng.range(-0.12, 0.12);
+        const double oy = rng.range(-0.12, 0.12);
+        const double oz = rng.range(-0.12, 0.12);
+        D3 v0 = c + D3{ox, oy, oz};
         v0 = D3{std::min(std::max(v0.x, lo.x), lo.x + 1), std::min(std::max(v0.y, lo.y), lo.y + 1),
                 std::min(std::max(v0.z, lo.z), lo.z + 1)};
-        const D3 v1 = v0 + rng.range(0.01, 0.2) * rng.sphere();
-        const D3 v2 = v0 + rng.range(0.01, 0.2) * rng.sphere();
+        // one RNG call per statement: the evaluation order of operands is
+        // unspecified and differs between compilers' targets
+        const double l1 = rng.range(0.01, 0.2);
+        const D3 e1 = rng.sphere();
+        const double l2 = rng.range(0.01, 0.2);
+        const D3 e2 = rng.sphere();
+        const D3 v1 = v0 + l1 * e1;
+        const D3 v2 = v0 + l2 * e2;
         const D3 n = unit(cross(v1 - v0, v2 - v0));
         b.flat_tri(v0, v1, v2, n, kWhite);
     }

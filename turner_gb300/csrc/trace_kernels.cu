@@ -1,0 +1,275 @@
+// Wavefront path-tracing kernels for sm_103a (compiled with -fmad=false).
+//
+// One render pass over a chunk of whole pixels:
+//   k_camera   primary rays for every (pixel, sample) path        main.cpp:200-214
+//   per depth 0..max_depth:
+//     k_trace   closest hit of every queued ray                   kdtree.cpp:516-607
+//     k_shade   hit point, interpolated normal, offset, next-event
+//               shadow ray, bounce direction; appends live paths to
+//               the next queue (warp ballot + one atomic per warp)  pathtracer.cpp:14-102
+//     k_shadow  any-hit occlusion test; adds the direct term       pathtracer.cpp:44-58
+//   k_resolve  per-pixel mean over samples in sample order, then exposure and
+//              gamma                                              main.cpp:216-223
+// The radiance of a path is accumulated forward: L += T * diffuse *
+// direct / pi at every hit (when the light is visible) and L += T * bg on a
+// miss, with T *= diffuse * 2 cos(theta) per uniform bounce (diffuse for a
+// cosine bounce). This is the reference's recursion
+// L_k = diffuse * (direct / pi + 2 cos L_{k+1}) unrolled.
+#include "device.cuh"
+#include "kernels.h"
+
+namespace turner {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append: one atomicAdd per warp, slots in lane order. Must
+// be reached by every lane of the warp.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
+    if (mask == 0) return 0;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (static_cast<int>(lane_id()) == leader) base = atomicAdd(counter, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
+}
+
+__global__ void __launch_bounds__(kBlock) k_intersect(SceneView sc, const float* __restrict__ ox,
+                                                      const float* __restrict__ oy, const float* __restrict__ oz,
+                                                      const float* __restrict__ dx, const float* __restrict__ dy,
+                                                      const float* __restrict__ dz, uint64_t n,
+                                                      uint32_t* __restrict__ hit_id, float* __restrict__ hr,
+                                                      float* __restrict__ hs, float* __restrict__ ht, int fast) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 o = make_float3(ox[i], oy[i], oz[i]);
+    const float3 d = make_float3(dx[i], dy[i], dz[i]);
+    const Hit h = fast ? traverse<false, true>(sc, o, d, 0.f) : traverse<false, false>(sc, o, d, 0.f);
+    hit_id[i] = h.id;
+    hr[i] = h.id < kMiss ? h.r : kFltMax;
+    hs[i] = h.id < kMiss ? h.s : 0.f;
+    ht[i] = h.id < kMiss ? h.t : 0.f;
+}
+
+// Camera::raster2cam (lib/types.h:117-123) with jitter from the path's own
+// xorshift stream; the direction is not normalised.
+__global__ void __launch_bounds__(kBlock) k_camera(JobDev job, uint32_t first_pixel, uint32_t n_paths, RayQueue q,
+                                                   float4* __restrict__ L) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *q.count = n_paths;
+    if (i >= n_paths) return;
+    const uint32_t local_pixel = i / job.spp;
+    const uint32_t sample = i - local_pixel * job.spp;
+    const uint32_t pixel = first_pixel + local_pixel;
+    const uint32_t y = pixel / job.width, x = pixel - y * job.width;
+    uint64_t js, bs;
+    path_seeds(job.seed, uint64_t(pixel) * job.spp + sample, js, bs);
+    const float jx = xorshift_float(js);
+    const float jy = xorshift_float(js);
+    const float px = static_cast<float>(x) + jx, py = static_cast<float>(y) + jy;
+    const float w = static_cast<float>(job.width), h = static_cast<float>(job.height);
+    const float vx = -job.delta_x * (1 - 2 * px / w);
+    const float vy = job.delta_y * (1 - 2 * py / h);
+    const float vz = -1;
+    const float* m = job.trafo;
+    const float3 d = make_float3(m[0] * vx + m[1] * vy + m[2] * vz, m[3] * vx + m[4] * vy + m[5] * vz,
+                                 m[6] * vx + m[7] * vy + m[8] * vz);
+    q.o[i] = make_float4(job.cam_pos[0], job.cam_pos[1], job.cam_pos[2], __uint_as_float(i));
+    q.d[i] = make_float4(d.x, d.y, d.z, 0.f);
+    q.T[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+    q.rng[i] = make_uint2(static_cast<uint32_t>(bs), static_cast<uint32_t>(bs >> 32));
+    L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(kBlock) k_trace(SceneView sc, RayQueue q, Hit* __restrict__ hits, int fast) {
+    const uint32_t n = *q.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = q.o[i];
+        const float4 d = q.d[i];
+        const float3 o3 = make_float3(o.x, o.y, o.z), d3 = make_float3(d.x, d.y, d.z);
+        hits[i] = fast ? traverse<false, true>(sc, o3, d3, 0.f) : traverse<false, false>(sc, o3, d3, 0.f);
+    }
+}
+
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 scale4(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+
+__global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueue in, const Hit* __restrict__ hits,
+                                                  RayQueue out, ShadowQueue sh, float4* __restrict__ L) {
+    const uint32_t n = *in.count;
+    const bool bounce_allowed = depth < job.max_depth && job.mc > 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // warp-uniform loop so every lane reaches the ballots
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t i = base + lane_id();
+        const bool valid = i < n;
+        bool emit_shadow = false, emit_bounce = false;
+        float4 sh_o, sh_d, sh_c, b_o, b_d, b_T;
+        uint2 b_rng;
+        if (valid) {
+            const Hit h = hits[i];
+            const float4 o4 = in.o[i];
+            const uint32_t path = __float_as_uint(o4.w);
+            const float4 T = in.T[i];
+            if (h.id >= kMiss) {
+                // miss: trace() returns conf.bg_color (alpha 1)
+                L[path] = add4(L[path], mul4(T, make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f)));
+            } else {
+                const float4 d4 = in.d[i];
+                const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
+                const float4* rec = job.sc.shade + 4 * size_t(h.id);
+                const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2), s3 = __ldg(rec + 3);
+                const float4 diffuse = make_float4(s0.w, s1.w, s2.w, s3.x);
+                // Triangle::interpolate_normal(1 - s - t, s, t) (lib/triangle.h:54-56)
+                const float w0 = 1.f - h.s - h.t;
+                const float nx = w0 * s0.x + h.s * s1.x + h.t * s2.x;
+                const float ny = w0 * s0.y + h.s * s1.y + h.t * s2.y;
+                const float nz = w0 * s0.z + h.s * s1.z + h.t * s2.z;
+                const float inv_len = 1 / sqrtf(nx * nx + ny * ny + nz * nz);
+                const float3 nrm = make_float3(inv_len * nx, inv_len * ny, inv_len * nz);
+                const float3 p2 = make_float3(p.x + 0.0001f * nrm.x, p.y + 0.0001f * nrm.y, p.z + 0.0001f * nrm.z);
+                const float4 Td = mul4(T, diffuse);
+                if (job.n_lights > 0) {
+                    const float lx = job.light_pos[0] - p.x, ly = job.light_pos[1] - p.y, lz = job.light_pos[2] - p.z;
+                    const float inv_l = 1 / sqrtf(lx * lx + ly * ly + lz * lz);
+                    const float3 ld = make_float3(inv_l * lx, inv_l * ly, inv_l * lz);
+                    const float qx = job.light_pos[0] - p2.x, qy = job.light_pos[1] - p2.y, qz = job.light_pos[2] - p2.z;
+                    const float dist = sqrtf(qx * qx + qy * qy + qz * qz);
+                    const float c = fmaxf(0.f, ld.x * nrm.x + ld.y * nrm.y + ld.z * nrm.z);
+                    if (c > 0.f) {
+                        // a zero cosine contributes nothing whether or not the light is blocked
+                        const float4 direct = scale4(c, make_float4(job.light_col[0], job.light_col[1],
+                                                                    job.light_col[2], job.light_col[3]));
+                        sh_c = mul4(Td, scale4(0.318309886183790671538f, direct));
+                        sh_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
+                        sh_d = make_float4(ld.x, ld.y, ld.z, dist);
+                        emit_shadow = true;
+                    }
+                }
+                if (bounce_allowed) {
+                    float m[9];
+                    from_to_z(nrm, m);
+                    const uint2 r2 = in.rng[i];
+                    uint64_t rs = uint64_t(r2.x) | (uint64_t(r2.y) << 32);
+                    const float u1 = xorshift_float(rs);
+                    const float u2 = xorshift_float(rs);
+                    float x, y, z, weight;
+                    if (job.sampling == 0) {
+                        // sampling::hemisphere (lib/sampling.h:20-32)
+                        z = u1;
+                        const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+                        const float phi = 6.28318548202514648438f * u2;
+                        x = rr * cosf(phi);
+                        y = rr * sinf(phi);
+                        weight = 2.f * u1;
+                    } else {
+                        const float rr = sqrtf(u1);
+                        z = sqrtf(fmaxf(0.f, 1.f - u1));
+                        const float phi = 6.28318548202514648438f * u2;
+                        x = rr * cosf(phi);
+                        y = rr * sinf(phi);
+                        weight = 1.f;
+                    }
+                    const float3 dir = make_float3(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
+                                                   m[6] * x + m[7] * y + m[8] * z);
+                    b_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
+                    b_d = make_float4(dir.x, dir.y, dir.z, 0.f);
+                    b_T = scale4(weight, Td);
+                    b_rng = make_uint2(static_cast<uint32_t>(rs), static_cast<uint32_t>(rs >> 32));
+                    emit_bounce = true;
+                }
+            }
+        }
+        const uint32_t si = warp_append(sh.count, emit_shadow);
+        if (emit_shadow) {
+            sh.o[si] = sh_o;
+            sh.d[si] = sh_d;
+            sh.c[si] = sh_c;
+        }
+        const uint32_t bi = warp_append(out.count, emit_bounce);
+        if (emit_bounce) {
+            out.o[bi] = b_o;
+            out.d[bi] = b_d;
+            out.T[bi] = b_T;
+            out.rng[bi] = b_rng;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_shadow(SceneView sc, ShadowQueue sh, float4* __restrict__ L) {
+    const uint32_t n = *sh.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = sh.o[i];
+        const float4 d = sh.d[i];
+        const Hit h = traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w);
+        if (h.id >= kMiss) {
+            const uint32_t path = __float_as_uint(o.w);
+            L[path] = add4(L[path], sh.c[i]);
+        }
+    }
+}
+
+// Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
+// on RGB; alpha is kept (lib/effects.h:15-49).
+__global__ void __launch_bounds__(kBlock) k_resolve(JobDev job, uint32_t first_pixel, uint32_t n_pixels,
+                                                    const float4* __restrict__ L, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pixels) return;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4* l = L + size_t(i) * job.spp;
+    for (uint32_t k = 0; k < job.spp; ++k) acc = add4(acc, l[k]);
+    const float fs = static_cast<float>(job.spp);
+    acc = make_float4(acc.x / fs, acc.y / fs, acc.z / fs, acc.w / fs);
+    if (job.tone_map) {
+        acc.x = 1 - expf(-acc.x * job.exposure);
+        acc.y = 1 - expf(-acc.y * job.exposure);
+        acc.z = 1 - expf(-acc.z * job.exposure);
+        if (job.gamma) {
+            acc.x = powf(acc.x, job.inv_gamma);
+            acc.y = powf(acc.y, job.inv_gamma);
+            acc.z = powf(acc.z, job.inv_gamma);
+        }
+    }
+    out[first_pixel + i] = acc;
+}
+
+inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
+
+} // namespace
+
+void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
+                      const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
+                      int fast, cudaStream_t stream) {
+    if (n == 0) return;
+    k_intersect<<<grid_for(n), kBlock, 0, stream>>>(sc, ox, oy, oz, dx, dy, dz, n, id, r, s, t, fast);
+}
+
+void launch_camera(const JobDev& job, uint32_t first_pixel, uint32_t n_paths, const RayQueue& q, float4* L,
+                   cudaStream_t stream) {
+    k_camera<<<grid_for(n_paths), kBlock, 0, stream>>>(job, first_pixel, n_paths, q, L);
+}
+
+void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast, cudaStream_t stream) {
+    k_trace<<<grid_for(capacity), kBlock, 0, stream>>>(sc, q, hits, fast);
+}
+
+void launch_shade(const JobDev& job, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
+                  const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream) {
+    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(job, depth, in, hits, out, sh, L);
+}
+
+void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream) {
+    k_shadow<<<grid_for(capacity), kBlock, 0, stream>>>(sc, sh, L);
+}
+
+void launch_resolve(const JobDev& job, uint32_t first_pixel, uint32_t n_pixels, const float4* L, float4* out,
+                    cudaStream_t stream) {
+    k_resolve<<<grid_for(n_pixels), kBlock, 0, stream>>>(job, first_pixel, n_pixels, L, out);
+}
+
+} // namespace turner
