@@ -179,7 +179,13 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-rows", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="480x270 frame of the same scene (for profiler captures; not a bench line)")
     args = ap.parse_args()
+    if args.small:
+        global WIDTH, HEIGHT, WORKLOAD
+        WIDTH, HEIGHT = 480, 270
+        WORKLOAD = "sphere_room_327k_480x270_16spp_d3 (profiling case)"
     if args.impl == "reference":
         run_reference(args)
         return

@@ -149,6 +149,11 @@ uint64_t turner_launch_count(turner_ctx* ctx);
 /* Paths in flight per render pass (queue length), >= 1024. Default 2^24.
  * No reference counterpart: the reference renders one row per task. */
 int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths);
+/* Traversal launch shape. persistent != 0 (default): resident blocks whose
+ * lanes take a new ray as soon as their current one finishes; blocks_per_sm
+ * caps the resident blocks (0 = occupancy limit, at most 64). persistent == 0:
+ * one thread per ray. No reference counterpart: tuning knob of this library. */
+int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks_per_sm);
 
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the

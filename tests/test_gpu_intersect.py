@@ -71,6 +71,20 @@ def test_fast_mode_matches_parity(ctx, uploaded, name):
     assert_same(ctx.intersect(sid, o, d, mode=tg.TRAVERSAL_FAST), ref.intersect(o, d))
 
 
+@pytest.mark.parametrize("persistent,blocks", [(False, 0), (True, 0), (True, 1), (True, 3)])
+def test_launch_shapes_agree(ctx, uploaded, persistent, blocks):
+    """One thread per ray, or persistent lanes with ray replacement at any
+    number of resident blocks: the same bit-exact answers."""
+    sid, ref, box = uploaded["soup20k"]
+    o, d = tg.make_rays(100_000, box, seed=31)
+    ctx.set_traversal_launch(persistent, blocks)
+    try:
+        gpu = ctx.intersect(sid, o, d)
+    finally:
+        ctx.set_traversal_launch(True, 0)
+    assert_same(gpu, ref.intersect(o, d))
+
+
 def test_reference_fixture_scenes(ctx):
     """The reference's kd-tree tests (tests/test_kdtree.cpp) on the GPU."""
     kd = dict(np.load(GOLD / "ref_kdtree_tests.npz"))

@@ -103,6 +103,20 @@ def test_chunking_is_invisible(ctx):
     assert np.array_equal(a, b) and sa.rays == sb.rays
 
 
+def test_launch_shape_is_invisible(ctx):
+    """Persistent traversal with ray replacement and one thread per ray render
+    the same image."""
+    m, sid, _ = setup(ctx, kind=tg.SCENE_SPHERE_ROOM, detail=4)
+    job = tg.make_job(sid, m, 48, 32, pixel_samples=2, max_depth=3, seed=12)
+    (a,), (sa,) = ctx.render([job])
+    ctx.set_traversal_launch(False, 0)
+    try:
+        (b,), (sb,) = ctx.render([job])
+    finally:
+        ctx.set_traversal_launch(True, 0)
+    assert np.array_equal(a, b) and sa.rays == sb.rays
+
+
 def test_render_is_deterministic(ctx):
     m, sid, _ = setup(ctx, kind=tg.SCENE_ROOM)
     job = tg.make_job(sid, m, 32, 32, pixel_samples=4, max_depth=3, seed=8)

@@ -102,6 +102,7 @@ def _lib() -> C.CDLL:
         "turner_launch_count": (C.c_uint64, [_P]),
         "turner_set_chunk_paths": (C.c_int, [_P, C.c_uint32]),
         "turner_set_profiling": (C.c_int, [_P, C.c_int]),
+        "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
@@ -270,6 +271,10 @@ class Context:
 
     def set_chunk_paths(self, paths: int) -> None:
         _check(_lib().turner_set_chunk_paths(self._h, paths), "turner_set_chunk_paths")
+
+    def set_traversal_launch(self, persistent: bool = True, blocks_per_sm: int = 0) -> None:
+        _check(_lib().turner_set_traversal_launch(self._h, 1 if persistent else 0, blocks_per_sm),
+               "turner_set_traversal_launch")
 
     def set_profiling(self, on: bool) -> None:
         _check(_lib().turner_set_profiling(self._h, 1 if on else 0), "turner_set_profiling")

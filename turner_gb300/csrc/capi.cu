@@ -58,7 +58,8 @@ struct turner_ctx {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
     // render workspace
-    DevBuf L, qa[4], qb[4], hits, shq[3], counters, image, rays_in, rays_out;
+    DevBuf L, qa[4], qb[4], hits, shq[3], counters, image, rays_in, rays_out, work;
+    TraverseCfg traverse;              // persistent traversal on by default
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
     uint64_t launches = 0;
@@ -358,10 +359,16 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
     TURNER_CK(cudaSetDevice(ctx->device));
     const SceneView& sc = ctx->scenes[scene_id]->view;
     const int fast = mode == TURNER_TRAVERSAL_FAST;
+    TURNER_CK(ctx->work.ensure(sizeof(uint32_t) * 64));
+    TraverseCfg cfg = ctx->traverse;
+    cfg.work = ctx->work.as<uint32_t>();
     if (flags == TURNER_DEVICE_BUFFERS) {
-        {
+        for (uint64_t b = 0; b < n; b += (1ull << 30)) {
+            const uint64_t m = std::min<uint64_t>(n - b, 1ull << 30);
+            TURNER_CK(cudaMemsetAsync(cfg.work, 0, sizeof(uint32_t), ctx->stream));
             KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);
-            launch_intersect(sc, ox, oy, oz, dx, dy, dz, n, hit_id, r, s, t, fast, ctx->stream);
+            launch_intersect(sc, ox + b, oy + b, oz + b, dx + b, dy + b, dz + b, m, hit_id + b, r + b, s + b, t + b,
+                             fast, cfg, ctx->stream);
         }
         TURNER_CK(cudaGetLastError());
         TURNER_CK(cudaStreamSynchronize(ctx->stream));
@@ -381,11 +388,12 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
             TURNER_CK(cudaMemcpyAsync(din + k * slice, src[k] + b, m * sizeof(float), cudaMemcpyHostToDevice,
                                       ctx->stream));
         }
+        TURNER_CK(cudaMemsetAsync(cfg.work, 0, sizeof(uint32_t), ctx->stream));
         {
             KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);
             launch_intersect(sc, din, din + slice, din + 2 * slice, din + 3 * slice, din + 4 * slice,
                              din + 5 * slice, m, reinterpret_cast<uint32_t*>(dout), dout + slice, dout + 2 * slice,
-                             dout + 3 * slice, fast, ctx->stream);
+                             dout + 3 * slice, fast, cfg, ctx->stream);
         }
         TURNER_CK(cudaGetLastError());
         TURNER_CK(cudaMemcpyAsync(hit_id + b, dout, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -401,6 +409,13 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
 int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths) {
     if (!ctx || paths < 1024) return TURNER_ERR_INVALID_ARG;
     ctx->chunk_paths = paths;
+    return TURNER_OK;
+}
+
+int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks_per_sm) {
+    if (!ctx || blocks_per_sm > 64) return TURNER_ERR_INVALID_ARG;
+    ctx->traverse.persistent = persistent != 0;
+    ctx->traverse.blocks_per_sm = blocks_per_sm;
     return TURNER_OK;
 }
 
@@ -434,14 +449,16 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
         TURNER_CK(ctx->qb[3].ensure(sizeof(uint2) * cap));
         TURNER_CK(ctx->hits.ensure(sizeof(Hit) * cap));
         const uint64_t n_chunks = (n_pixels + px_per_chunk - 1) / px_per_chunk;
-        TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * 2 * (levels + 1) * n_chunks));
+        // per chunk: [queued rays | shadow rays | trace work | shadow work], levels + 1 slots each
+        const size_t stride = 4 * size_t(levels + 1);
+        TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * stride * n_chunks));
         float4* image = reinterpret_cast<float4*>(out_rgba[j]);
         if (flags == TURNER_HOST_BUFFERS) {
             TURNER_CK(ctx->image.ensure(sizeof(float4) * n_pixels));
             image = ctx->image.as<float4>();
         }
         uint32_t* counters = ctx->counters.as<uint32_t>();
-        TURNER_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * 2 * (levels + 1) * n_chunks, ctx->stream));
+        TURNER_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * stride * n_chunks, ctx->stream));
         TURNER_CK(cudaEventRecord(ctx->ev0, ctx->stream));
 
         RayQueue qa{ctx->qa[0].as<float4>(), ctx->qa[1].as<float4>(), ctx->qa[2].as<float4>(), ctx->qa[3].as<uint2>(),
@@ -453,7 +470,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
             const uint32_t first = static_cast<uint32_t>(c * px_per_chunk);
             const uint32_t npx = static_cast<uint32_t>(std::min<uint64_t>(px_per_chunk, n_pixels - first));
             const uint32_t n_paths = npx * job.pixel_samples;
-            uint32_t* cnt = counters + 2 * (levels + 1) * c;   // [ray counts per level | shadow counts per level]
+            uint32_t* cnt = counters + stride * c;
             RayQueue cur = qa, nxt = qb;
             cur.count = cnt;
             {
@@ -463,10 +480,13 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
             for (int depth = 0; depth <= job.max_depth; ++depth) {
                 nxt.count = cnt + depth + 1;
                 sh.count = cnt + (levels + 1) + depth;
+                TraverseCfg trace_cfg = ctx->traverse, shadow_cfg = ctx->traverse;
+                trace_cfg.work = cnt + 2 * (levels + 1) + depth;
+                shadow_cfg.work = cnt + 3 * (levels + 1) + depth;
                 {
                     KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
                     launch_trace(jd.sc, cur, ctx->hits.as<Hit>(), n_paths, job.traversal == TURNER_TRAVERSAL_FAST,
-                                 ctx->stream);
+                                 trace_cfg, ctx->stream);
                 }
                 {
                     KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
@@ -475,7 +495,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
                 }
                 {
                     KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
-                    launch_shadow(jd.sc, sh, ctx->L.as<float4>(), n_paths, ctx->stream);
+                    launch_shadow(jd.sc, sh, ctx->L.as<float4>(), n_paths, shadow_cfg, ctx->stream);
                 }
                 std::swap(cur, nxt);
             }
@@ -490,7 +510,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
             TURNER_CK(cudaMemcpyAsync(out_rgba[j], image, sizeof(float4) * n_pixels, cudaMemcpyDeviceToHost,
                                       ctx->stream));
         }
-        std::vector<uint32_t> host_cnt(2 * (levels + 1) * n_chunks);
+        std::vector<uint32_t> host_cnt(stride * n_chunks);
         TURNER_CK(cudaMemcpyAsync(host_cnt.data(), counters, sizeof(uint32_t) * host_cnt.size(),
                                   cudaMemcpyDeviceToHost, ctx->stream));
         TURNER_CK(cudaStreamSynchronize(ctx->stream));
@@ -499,7 +519,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
             turner_stats& st = stats[j];
             st.rays = st.primary_rays = st.shadow_rays = 0;
             for (uint64_t c = 0; c < n_chunks; ++c) {
-                const uint32_t* cc = host_cnt.data() + 2 * (levels + 1) * c;
+                const uint32_t* cc = host_cnt.data() + stride * c;
                 st.primary_rays += cc[0];
                 for (int k = 0; k < levels; ++k) {
                     st.rays += cc[k];

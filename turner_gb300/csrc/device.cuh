@@ -166,6 +166,115 @@ __device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d,
     return best;
 }
 
+// Resumable form of traverse() for persistent kernels: the same visit order
+// and arithmetic, split into rounds so that a lane can take a new ray as soon
+// as its current one is finished (ray replacement, Aila & Laine 2009).
+struct TravState {
+    float3 o, d, inv;
+    uint32_t neg;    // bit ax: fixed direction component <= 0 (near child is the right one)
+    uint32_t node;
+    float tenter, texit;
+    int sp;
+    Hit best;
+};
+
+// fix_direction + root box test. false: the ray misses the scene box.
+__device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3 d, TravState& s) {
+    s.best = Hit{kMiss, kFltMax, 0.f, 0.f};
+    const float3 fd = make_float3(d.x == 0.f ? kEps : d.x, d.y == 0.f ? kEps : d.y, d.z == 0.f ? kEps : d.z);
+    s.o = o;
+    s.d = d;
+    s.inv = make_float3(1.0f / fd.x, 1.0f / fd.y, 1.0f / fd.z);
+    s.neg = (fd.x <= 0.f ? 1u : 0u) | (fd.y <= 0.f ? 2u : 0u) | (fd.z <= 0.f ? 4u : 0u);
+    const float tx1 = (sc.lo[0] - o.x) * s.inv.x, tx2 = (sc.hi[0] - o.x) * s.inv.x;
+    float tenter = fminf(tx1, tx2);
+    float texit = fmaxf(tx1, tx2);
+    const float ty1 = (sc.lo[1] - o.y) * s.inv.y, ty2 = (sc.hi[1] - o.y) * s.inv.y;
+    tenter = fmaxf(tenter, fminf(ty1, ty2));
+    texit = fminf(texit, fmaxf(ty1, ty2));
+    const float tz1 = (sc.lo[2] - o.z) * s.inv.z, tz2 = (sc.hi[2] - o.z) * s.inv.z;
+    tenter = fmaxf(tenter, fminf(tz1, tz2));
+    texit = fminf(texit, fmaxf(tz1, tz2));
+    s.tenter = tenter;
+    s.texit = texit;
+    s.node = 0;
+    s.sp = 0;
+    return !(texit < tenter);
+}
+
+// One round: descend from s.node to a leaf, test its run, pop the next cell.
+// Returns true when the ray is finished (s.best holds the answer).
+template <bool ANY, bool FAST_EXIT>
+__device__ __forceinline__ bool trav_round(const SceneView& sc, TravState& s, float tmax, uint32_t* st_node,
+                                           float* st_enter, float* st_exit) {
+    const uint2* __restrict__ nodes = sc.nodes;
+    uint32_t node = s.node;
+    float tenter = s.tenter, texit = s.texit;
+    int sp = s.sp;
+    uint2 w = __ldg(nodes + node);
+    while ((w.x & 3u) != 3u) {
+        const uint32_t ax = w.x & 3u;
+        const float t = (__uint_as_float(w.y) - pick(s.o, ax)) * pick(s.inv, ax);
+        uint32_t near_c = node + 1, far_c = w.x >> 2;
+        if (s.neg & (1u << ax)) {
+            const uint32_t tmp = near_c;
+            near_c = far_c;
+            far_c = tmp;
+        }
+        if (texit < t) {
+            node = near_c;
+        } else if (t < tenter) {
+            node = far_c;
+        } else {
+            st_node[sp] = far_c;
+            st_enter[sp] = t;
+            st_exit[sp] = texit;
+            ++sp;
+            node = near_c;
+            texit = t;
+        }
+        w = __ldg(nodes + node);
+    }
+    for (;;) {
+        float r, u, v;
+        if (triangle_test(sc.tri, w.y, s.o, s.d, r, u, v)) {
+            if (ANY) {
+                if (r <= tmax) {
+                    s.best = Hit{w.y, r, u, v};
+                    return true;
+                }
+            } else if (r < s.best.r) {
+                s.best = Hit{w.y, r, u, v};
+            }
+        }
+        if (w.x == 0xFFFFFFFFu) break;
+        const uint32_t id2 = w.x >> 2;
+        if (triangle_test(sc.tri, id2, s.o, s.d, r, u, v)) {
+            if (ANY) {
+                if (r <= tmax) {
+                    s.best = Hit{id2, r, u, v};
+                    return true;
+                }
+            } else if (r < s.best.r) {
+                s.best = Hit{id2, r, u, v};
+            }
+        }
+        ++node;
+        w = __ldg(nodes + node);
+        if ((w.x & 3u) != 3u) break;
+    }
+    if (sp == 0) return true;
+    --sp;
+    if (FAST_EXIT && !ANY) {
+        if (s.best.r < st_enter[sp] - (1e-3f + 1e-3f * fabsf(st_enter[sp]))) return true;
+    }
+    s.node = st_node[sp];
+    s.tenter = st_enter[sp];
+    s.texit = st_exit[sp];
+    s.sp = sp;
+    return false;
+}
+
 // xorshift64* (lib/xorshift.h:27-70): float = (x & (2^24 - 1)) * 2^-24
 __device__ __forceinline__ float xorshift_float(uint64_t& s) {
     s ^= s >> 12;

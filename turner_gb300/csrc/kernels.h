@@ -44,15 +44,26 @@ struct JobDev {
     int32_t gamma, tone_map;
 };
 
+// How traversal kernels are launched. persistent: one grid of resident
+// blocks whose lanes pull rays from `work` (a zeroed device counter) until the
+// queue is empty; otherwise one thread per queue slot.
+struct TraverseCfg {
+    bool persistent = true;
+    unsigned blocks_per_sm = 0;   // 0: as many as are resident
+    uint32_t* work = nullptr;
+};
+
 void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                       const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
-                      int fast, cudaStream_t stream);
+                      int fast, const TraverseCfg& cfg, cudaStream_t stream);
 void launch_camera(const JobDev& job, uint32_t first_pixel, uint32_t n_paths, const RayQueue& q, float4* L,
                    cudaStream_t stream);
-void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast, cudaStream_t stream);
+void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast,
+                  const TraverseCfg& cfg, cudaStream_t stream);
 void launch_shade(const JobDev& job, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
                   const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream);
-void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream);
+void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, const TraverseCfg& cfg,
+                   cudaStream_t stream);
 void launch_resolve(const JobDev& job, uint32_t first_pixel, uint32_t n_pixels, const float4* L, float4* out,
                     cudaStream_t stream);
 

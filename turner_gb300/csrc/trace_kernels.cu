@@ -201,6 +201,112 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
     }
 }
 
+// ---------------------------------------------------------------- persistent
+// Ray sources for the persistent traversal kernel: where rays come from and
+// where the answer goes.
+struct QueueSrc {           // closest hit of a ray queue -> hit array
+    const float4* o;
+    const float4* d;
+    const uint32_t* cnt;
+    Hit* hits;
+    __device__ uint32_t count() const { return *cnt; }
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+        const float4 a = o[i], b = d[i];
+        o3 = make_float3(a.x, a.y, a.z);
+        d3 = make_float3(b.x, b.y, b.z);
+        tmax = 0.f;
+    }
+    __device__ void store(uint32_t i, const Hit& h) const { hits[i] = h; }
+};
+
+struct ShadowSrc {          // any hit of a shadow queue -> direct light if unblocked
+    const float4* o;
+    const float4* d;
+    const float4* c;
+    const uint32_t* cnt;
+    float4* L;
+    __device__ uint32_t count() const { return *cnt; }
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+        const float4 a = o[i], b = d[i];
+        o3 = make_float3(a.x, a.y, a.z);
+        d3 = make_float3(b.x, b.y, b.z);
+        tmax = b.w;
+    }
+    __device__ void store(uint32_t i, const Hit& h) const {
+        if (h.id >= kMiss) {
+            const uint32_t path = __float_as_uint(o[i].w);
+            const float4 ci = c[i];
+            float4 l = L[path];
+            L[path] = make_float4(l.x + ci.x, l.y + ci.y, l.z + ci.z, l.w + ci.w);
+        }
+    }
+};
+
+struct SoaSrc {             // turner_intersect batches
+    const float *ox, *oy, *oz, *dx, *dy, *dz;
+    uint32_t n;
+    uint32_t* id;
+    float *r, *s, *t;
+    __device__ uint32_t count() const { return n; }
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+        o3 = make_float3(ox[i], oy[i], oz[i]);
+        d3 = make_float3(dx[i], dy[i], dz[i]);
+        tmax = 0.f;
+    }
+    __device__ void store(uint32_t i, const Hit& h) const {
+        const bool hit = h.id < kMiss;
+        id[i] = h.id;
+        r[i] = hit ? h.r : kFltMax;
+        s[i] = hit ? h.s : 0.f;
+        t[i] = hit ? h.t : 0.f;
+    }
+};
+
+// Persistent traversal: each lane holds one ray; lanes whose ray is finished
+// take the next unclaimed ray (one atomicAdd per warp), so warps stay full
+// while rays of very different lengths are traversed.
+template <class Src, bool ANY, bool FAST>
+__global__ void __launch_bounds__(kBlock) k_traverse(SceneView sc, Src src, uint32_t* __restrict__ work) {
+    const uint32_t n = src.count();
+    uint32_t st_node[kStackCap];
+    float st_enter[kStackCap], st_exit[kStackCap];
+    TravState s;
+    uint32_t cur = 0;
+    bool active = false, exhausted = false;
+    float tmax = 0.f;
+    for (;;) {
+        for (;;) {
+            const bool need = !active && !exhausted;
+            const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
+            if (mask == 0) break;
+            const int leader = __ffs(mask) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane_id()) == leader) base = atomicAdd(work, static_cast<uint32_t>(__popc(mask)));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                const uint32_t idx = base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
+                if (idx >= n) {
+                    exhausted = true;
+                } else {
+                    float3 o, d;
+                    src.load(idx, o, d, tmax);
+                    if (trav_begin(sc, o, d, s)) {
+                        cur = idx;
+                        active = true;
+                    } else {
+                        src.store(idx, s.best);   // misses the scene box
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
+        if (active && trav_round<ANY, FAST>(sc, s, tmax, st_node, st_enter, st_exit)) {
+            src.store(cur, s.best);
+            active = false;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_shadow(SceneView sc, ShadowQueue sh, float4* __restrict__ L) {
     const uint32_t n = *sh.count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -240,12 +346,41 @@ __global__ void __launch_bounds__(kBlock) k_resolve(JobDev job, uint32_t first_p
 
 inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
+// Resident blocks per SM x SMs for a persistent kernel (cached per kernel).
+template <class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap) {
+    static int sms = 0, per_sm = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+        sms = std::max(1, sms);
+        per_sm = std::max(1, per_sm);
+    }
+    const unsigned per = blocks_per_sm_cap ? std::min<unsigned>(per_sm, blocks_per_sm_cap) : per_sm;
+    return static_cast<unsigned>(sms) * per;
+}
+
+template <class Src, bool ANY, bool FAST>
+void run_traverse(const SceneView& sc, const Src& src, uint32_t capacity, const TraverseCfg& cfg,
+                  cudaStream_t stream) {
+    auto kernel = k_traverse<Src, ANY, FAST>;
+    const unsigned grid = std::min(persistent_grid(kernel, cfg.blocks_per_sm), std::max(1u, grid_for(capacity)));
+    kernel<<<grid, kBlock, 0, stream>>>(sc, src, cfg.work);
+}
+
 } // namespace
 
 void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                       const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
-                      int fast, cudaStream_t stream) {
+                      int fast, const TraverseCfg& cfg, cudaStream_t stream) {
     if (n == 0) return;
+    if (cfg.persistent && n < (1ull << 31)) {
+        const SoaSrc src{ox, oy, oz, dx, dy, dz, static_cast<uint32_t>(n), id, r, s, t};
+        if (fast) run_traverse<SoaSrc, false, true>(sc, src, static_cast<uint32_t>(n), cfg, stream);
+        else run_traverse<SoaSrc, false, false>(sc, src, static_cast<uint32_t>(n), cfg, stream);
+        return;
+    }
     k_intersect<<<grid_for(n), kBlock, 0, stream>>>(sc, ox, oy, oz, dx, dy, dz, n, id, r, s, t, fast);
 }
 
@@ -254,7 +389,14 @@ void launch_camera(const JobDev& job, uint32_t first_pixel, uint32_t n_paths, co
     k_camera<<<grid_for(n_paths), kBlock, 0, stream>>>(job, first_pixel, n_paths, q, L);
 }
 
-void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast, cudaStream_t stream) {
+void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast,
+                  const TraverseCfg& cfg, cudaStream_t stream) {
+    if (cfg.persistent) {
+        const QueueSrc src{q.o, q.d, q.count, hits};
+        if (fast) run_traverse<QueueSrc, false, true>(sc, src, capacity, cfg, stream);
+        else run_traverse<QueueSrc, false, false>(sc, src, capacity, cfg, stream);
+        return;
+    }
     k_trace<<<grid_for(capacity), kBlock, 0, stream>>>(sc, q, hits, fast);
 }
 
@@ -263,7 +405,13 @@ void launch_shade(const JobDev& job, int depth, const RayQueue& in, const Hit* h
     k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(job, depth, in, hits, out, sh, L);
 }
 
-void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream) {
+void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, const TraverseCfg& cfg,
+                   cudaStream_t stream) {
+    if (cfg.persistent) {
+        const ShadowSrc src{sh.o, sh.d, sh.c, sh.count, L};
+        run_traverse<ShadowSrc, true, false>(sc, src, capacity, cfg, stream);
+        return;
+    }
     k_shadow<<<grid_for(capacity), kBlock, 0, stream>>>(sc, sh, L);
 }
 
