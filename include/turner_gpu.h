@@ -197,6 +197,28 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
                      const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id, float* r,
                      float* s, float* t, int mode, uint32_t flags);
 
+/* Batched intersect that allocates nothing. No counterpart in the reference.
+ * For callers that must not allocate device memory while they run: a
+ * renderer's per-frame loop (cudaMalloc can synchronize the whole device and
+ * stall the frame) or a host framework whose own pool owns every device
+ * allocation. They upload the scene once at load time, then pass rays and
+ * outputs in device memory they own (SoA as in turner_intersect with
+ * TURNER_DEVICE_BUFFERS); results are identical to turner_intersect.
+ * The traversal's scratch (its work counter) lives in a static device array
+ * of TURNER_NOALLOC_SCRATCH_WORDS 32-bit words that every GPU loading this
+ * library holds until exit; no cudaMalloc, cudaFree or allocating library
+ * call is made. The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress), so make the first call before any stream
+ * capture. All calls on a device share the array: calls that overlap on the
+ * GPU (other streams, other contexts) race and must be serialized by the
+ * caller. At most TURNER_NOALLOC_MAX_RAYS rays per call (the counter is 32
+ * bits); more return TURNER_ERR_TOO_LARGE. Synchronous on the context stream. */
+#define TURNER_NOALLOC_SCRATCH_WORDS 64
+#define TURNER_NOALLOC_MAX_RAYS (1ull << 30)
+int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
+                             const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id,
+                             float* r, float* s, float* t, int mode);
+
 /* -------------------------------------------------------------- render */
 /* Renders each job into out_rgba[j] (width*height*4 floats, row-major RGBA
  * after the per-pixel mean, exposure and gamma of main.cpp:216-223), host or

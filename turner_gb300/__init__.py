@@ -108,6 +108,7 @@ def _lib() -> C.CDLL:
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
         "turner_validate_nodes": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]),
         "turner_intersect": (C.c_int, [_P, C.c_uint32] + [_P] * 6 + [C.c_uint64] + [_P] * 4 + [C.c_int, C.c_uint32]),
+        "turner_intersect_noalloc": (C.c_int, [_P, C.c_uint32] + [_P] * 6 + [C.c_uint64] + [_P] * 4 + [C.c_int]),
         "turner_render": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.POINTER(_P), C.POINTER(Stats), C.c_uint32]),
         "turner_render_accumulate": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, _P, C.POINTER(C.c_uint64),
                                                C.c_uint32]),
@@ -319,6 +320,7 @@ class Context:
 
     def intersect_device(self, scene_id: int, ptrs: list[int], n: int, out_ptrs: list[int],
                          mode: int = TRAVERSAL_PARITY) -> None:
+        # ptrs: ox, oy, oz, dx, dy, dz; out_ptrs: id, r, s, t (device addresses)
         """Device-buffer batch intersect (six ray pointers, four output pointers)."""
         _check(_lib().turner_intersect(self._h, scene_id, *ptrs, n, *out_ptrs, mode, DEVICE_BUFFERS),
                "turner_intersect")

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -550,6 +551,71 @@ int turner_kernel_times(turner_ctx* ctx, double* ms, uint64_t* launches, int res
             ctx->kernel_launches[k] = 0;
         }
     }
+    return TURNER_OK;
+}
+
+} // extern "C"
+
+// ------------------------------------------------ no-allocation intersect
+// Scratch of turner_intersect_noalloc: word 0 is the work counter from which
+// the persistent traversal's lanes claim rays. The array fills one 256-byte
+// segment so that no other variable shares the cache lines of that heavily
+// contended atomic. Every GPU that loads this library holds these 256 bytes
+// until the process exits.
+static __device__ __align__(256) uint32_t g_noalloc_scratch[TURNER_NOALLOC_SCRATCH_WORDS];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device`, looked up once per device
+// with that device current. In host code the array's name only stands in for
+// the symbol; a kernel must be given this address instead.
+int noalloc_scratch(int device, uint32_t** out) {
+    if (device < 0 || device >= kMaxDevices) return TURNER_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return e != cudaSuccess ? map_cuda(e) : TURNER_ERR_CUDA;
+        g_noalloc_ptr[device] = static_cast<uint32_t*>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return TURNER_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
+                             const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id,
+                             float* r, float* s, float* t, int mode) {
+    if (!ctx || scene_id >= ctx->scenes.size() || !ctx->scenes[scene_id]->live) return TURNER_ERR_INVALID_ARG;
+    if (!ox || !oy || !oz || !dx || !dy || !dz || !hit_id || !r || !s || !t) return TURNER_ERR_INVALID_ARG;
+    if (mode != TURNER_TRAVERSAL_PARITY && mode != TURNER_TRAVERSAL_FAST) return TURNER_ERR_INVALID_ARG;
+    if (n > TURNER_NOALLOC_MAX_RAYS) return TURNER_ERR_TOO_LARGE;
+    if (n == 0) return TURNER_OK;
+    TURNER_CK(cudaSetDevice(ctx->device));
+    uint32_t* scratch = nullptr;
+    const int st = noalloc_scratch(ctx->device, &scratch);
+    if (st != TURNER_OK) {
+        ctx->last_error = "cudaGetSymbolAddress(g_noalloc_scratch) failed";
+        return st;
+    }
+    // the array keeps the previous call's counter: it must start at zero
+    TURNER_CK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t), ctx->stream));
+    TraverseCfg cfg;
+    cfg.persistent = true;
+    cfg.blocks_per_sm = ctx->traverse.blocks_per_sm;
+    cfg.work = scratch;
+    launch_intersect(ctx->scenes[scene_id]->view, ox, oy, oz, dx, dy, dz, n, hit_id, r, s, t,
+                     mode == TURNER_TRAVERSAL_FAST, cfg, ctx->stream);
+    ctx->launches += 1;
+    TURNER_CK(cudaGetLastError());
+    TURNER_CK(cudaStreamSynchronize(ctx->stream));
     return TURNER_OK;
 }
 
