@@ -119,8 +119,15 @@ typedef struct turner_job {
     turner_light light;
     turner_camera camera;
     int32_t sampling;             /* TURNER_SAMPLING_*                        */
-    int32_t traversal;            /* TURNER_TRAVERSAL_* for bounce rays       */
+    int32_t traversal;            /* TURNER_TRAVERSAL_* for bounce rays; a batch
+                                     uses FAST only if every job asks for it  */
+    int32_t linear_output;        /* 1: write the per-pixel mean radiance
+                                     without exposure and gamma (for error
+                                     measurements against converged images) */
 } turner_job;
+
+/* Jobs per turner_render call. */
+#define TURNER_MAX_JOBS 4096
 
 typedef struct turner_stats {
     uint64_t rays;          /* reference count: traced rays at depth <= max_depth,
@@ -222,11 +229,19 @@ int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox
 /* -------------------------------------------------------------- render */
 /* Renders each job into out_rgba[j] (width*height*4 floats, row-major RGBA
  * after the per-pixel mean, exposure and gamma of main.cpp:216-223), host or
- * device memory per `flags`. All jobs go through one wavefront launch
- * sequence (one CUDA graph when n_jobs > 1). stats may be NULL; otherwise it
- * receives one turner_stats per job. Synchronous. */
+ * device memory per `flags`. All jobs of a call form one batch: their pixels
+ * are laid end to end and traced in passes of up to the chunk length (a pass
+ * may hold pixels of several jobs of different scenes, sizes, sample counts
+ * and depths); a batch of more than one job is captured into one CUDA graph
+ * and launched once. stats may be NULL; otherwise it receives one
+ * turner_stats per job (device_ms is the whole batch's). Synchronous. */
 int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float* const* out_rgba,
                   turner_stats* stats, uint32_t flags);
+/* Capture single-job renders into a CUDA graph too (always != 0). No
+ * reference counterpart. */
+int turner_set_graph_mode(turner_ctx* ctx, int always);
+/* Number of CUDA graphs launched by this context. No reference counterpart. */
+uint64_t turner_graph_launch_count(turner_ctx* ctx);
 
 /* Progressive FP64 accumulation for converged reference images: adds
  * `passes` further sample passes of pixel_samples each to a double-precision

@@ -73,7 +73,8 @@ class Job(C.Structure):
                 ("pixel_samples", C.c_uint32), ("max_depth", C.c_int32), ("monte_carlo_samples", C.c_int32),
                 ("exposure", C.c_float), ("inverse_gamma", C.c_float), ("gamma_correction", C.c_int32),
                 ("background", C.c_float * 3), ("seed", C.c_uint64), ("n_lights", C.c_int32),
-                ("light", Light), ("camera", Camera), ("sampling", C.c_int32), ("traversal", C.c_int32)]
+                ("light", Light), ("camera", Camera), ("sampling", C.c_int32), ("traversal", C.c_int32),
+                ("linear_output", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -102,6 +103,8 @@ def _lib() -> C.CDLL:
         "turner_launch_count": (C.c_uint64, [_P]),
         "turner_set_chunk_paths": (C.c_int, [_P, C.c_uint32]),
         "turner_set_profiling": (C.c_int, [_P, C.c_int]),
+        "turner_set_graph_mode": (C.c_int, [_P, C.c_int]),
+        "turner_graph_launch_count": (C.c_uint64, [_P]),
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
@@ -324,6 +327,21 @@ class Context:
         """Device-buffer batch intersect (six ray pointers, four output pointers)."""
         _check(_lib().turner_intersect(self._h, scene_id, *ptrs, n, *out_ptrs, mode, DEVICE_BUFFERS),
                "turner_intersect")
+
+    def set_graph_mode(self, always: bool) -> None:
+        _check(_lib().turner_set_graph_mode(self._h, 1 if always else 0), "turner_set_graph_mode")
+
+    def graph_launch_count(self) -> int:
+        return _lib().turner_graph_launch_count(self._h)
+
+    def accumulate(self, job: Job, passes: int) -> tuple[np.ndarray, int]:
+        """FP64 running mean of linear radiance after `passes` more passes of
+        job.pixel_samples samples each: ((h, w, 4) float64, total samples)."""
+        out = np.empty((job.height, job.width, 4), np.float64)
+        total = C.c_uint64(0)
+        _check(_lib().turner_render_accumulate(self._h, C.byref(job), passes, _ptr(out), C.byref(total),
+                                               HOST_BUFFERS), "turner_render_accumulate")
+        return out, total.value
 
     def render(self, jobs: list[Job], outs: list[int] | None = None, flags: int = HOST_BUFFERS):
         """Renders jobs; returns (images, stats). With flags=DEVICE_BUFFERS,

@@ -59,7 +59,11 @@ struct turner_ctx {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
     // render workspace
-    DevBuf L, qa[4], qb[4], hits, shq[3], counters, image, rays_in, rays_out, work;
+    DevBuf L, qa[4], qb[4], hits, shq[3], shjob, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc;
+    uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
+    uint64_t acc_samples = 0, acc_passes = 0;
+    bool use_graph = false;            // capture single-job renders too
+    uint64_t graph_launches = 0;
     TraverseCfg traverse;              // persistent traversal on by default
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
@@ -171,7 +175,7 @@ long validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris) {
     return h[0];
 }
 
-void fill_job(const turner_job& j, const SceneView& sc, JobDev& d) {
+void fill_job(const turner_job& j, const SceneView& sc, JobDesc& d) {
     std::memset(&d, 0, sizeof(d));
     d.sc = sc;
     std::memcpy(d.cam_pos, j.camera.position, sizeof(d.cam_pos));
@@ -420,120 +424,292 @@ int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks
     return TURNER_OK;
 }
 
+} // extern "C"
+
+namespace {
+
+// A batch of jobs laid out for one launch sequence: the device job table,
+// the pixel chunks (passes) and the workspace size.
+struct Batch {
+    std::vector<JobDesc> table;
+    std::vector<Chunk> chunks;
+    uint64_t total_pixels = 0;
+    uint32_t cap = 0;                // paths per pass
+    int levels = 0;                  // largest max_depth + 1
+    bool single_scene = true;
+    SceneView single{};
+};
+
+int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4* const* outs, bool tone_map,
+               Batch& b) {
+    b.table.resize(n_jobs);
+    uint64_t pixels = 0, paths = 0;
+    uint32_t max_spp = 1;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        fill_job(jobs[j], ctx->scenes[jobs[j].scene_id]->view, b.table[j]);
+        JobDesc& d = b.table[j];
+        d.tone_map = tone_map ? 1 : 0;
+        d.pixel_offset = pixels;
+        d.path_offset = paths;
+        d.out = outs ? outs[j] : nullptr;
+        pixels += uint64_t(d.width) * d.height;
+        paths += uint64_t(d.width) * d.height * d.spp;
+        max_spp = std::max(max_spp, d.spp);
+        b.levels = std::max(b.levels, d.max_depth + 1);
+        if (jobs[j].scene_id != jobs[0].scene_id) b.single_scene = false;
+    }
+    b.total_pixels = pixels;
+    b.single = b.table[0].sc;
+    b.cap = static_cast<uint32_t>(std::min<uint64_t>(paths, std::max<uint64_t>(ctx->chunk_paths, max_spp)));
+    // whole pixels, at most cap paths per chunk; a chunk may span several jobs
+    Chunk c{0, 0, 0, 0};
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const JobDesc& d = b.table[j];
+        uint64_t left = uint64_t(d.width) * d.height;
+        while (left > 0) {
+            const uint64_t room = (b.cap - c.n_paths) / d.spp;
+            if (room == 0) {
+                b.chunks.push_back(c);
+                c = Chunk{c.pixel0 + c.n_pixels, c.path0 + c.n_paths, 0, 0};
+                continue;
+            }
+            const uint64_t take = std::min(room, left);
+            c.n_pixels += static_cast<uint32_t>(take);
+            c.n_paths += static_cast<uint32_t>(take * d.spp);
+            left -= take;
+        }
+    }
+    if (c.n_pixels) b.chunks.push_back(c);
+    return TURNER_OK;
+}
+
+int ensure_workspace(turner_ctx* ctx, const Batch& b) {
+    const uint32_t cap = b.cap;
+    TURNER_CK(ctx->L.ensure(sizeof(float4) * cap));
+    for (int k = 0; k < 3; ++k) {
+        TURNER_CK(ctx->qa[k].ensure(sizeof(float4) * cap));
+        TURNER_CK(ctx->qb[k].ensure(sizeof(float4) * cap));
+        TURNER_CK(ctx->shq[k].ensure(sizeof(float4) * cap));
+    }
+    TURNER_CK(ctx->qa[3].ensure(sizeof(uint2) * cap));
+    TURNER_CK(ctx->qb[3].ensure(sizeof(uint2) * cap));
+    TURNER_CK(ctx->shjob.ensure(sizeof(uint32_t) * cap));
+    TURNER_CK(ctx->hits.ensure(sizeof(Hit) * cap));
+    TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * 4 * size_t(b.levels + 1) * b.chunks.size()));
+    TURNER_CK(ctx->jobtab.ensure(sizeof(JobDesc) * b.table.size()));
+    TURNER_CK(ctx->jobcnt.ensure(sizeof(unsigned long long) * 2 * b.table.size()));
+    return TURNER_OK;
+}
+
+// Every launch of the batch on ctx->stream, no host synchronization (so the
+// sequence can be captured into a CUDA graph). acc != nullptr: accumulate
+// linear radiance in FP64 instead of resolving images.
+int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
+    const size_t stride = 4 * size_t(b.levels + 1);
+    uint32_t* counters = ctx->counters.as<uint32_t>();
+    const JobDesc* jobs = ctx->jobtab.as<JobDesc>();
+    const uint32_t n_jobs = static_cast<uint32_t>(b.table.size());
+    unsigned long long* job_counts = ctx->jobcnt.as<unsigned long long>();
+    TURNER_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * stride * b.chunks.size(), ctx->stream));
+    TURNER_CK(cudaMemsetAsync(job_counts, 0, sizeof(unsigned long long) * 2 * n_jobs, ctx->stream));
+    const SceneView* single = b.single_scene ? &b.single : nullptr;
+    int fast = 1;
+    for (const JobDesc& d : b.table) fast &= d.traversal == TURNER_TRAVERSAL_FAST ? 1 : 0;
+    const RayQueue qa{ctx->qa[0].as<float4>(), ctx->qa[1].as<float4>(), ctx->qa[2].as<float4>(),
+                      ctx->qa[3].as<uint2>(), nullptr};
+    const RayQueue qb{ctx->qb[0].as<float4>(), ctx->qb[1].as<float4>(), ctx->qb[2].as<float4>(),
+                      ctx->qb[3].as<uint2>(), nullptr};
+    ShadowQueue sh{ctx->shq[0].as<float4>(), ctx->shq[1].as<float4>(), ctx->shq[2].as<float4>(),
+                   ctx->shjob.as<uint32_t>(), nullptr};
+    for (size_t ci = 0; ci < b.chunks.size(); ++ci) {
+        const Chunk& c = b.chunks[ci];
+        uint32_t* cnt = counters + stride * ci;   // [queued rays | shadow rays | trace work | shadow work]
+        RayQueue cur = qa, nxt = qb;
+        cur.count = cnt;
+        {
+            KernelTimer kt(ctx, TURNER_KERNEL_CAMERA);
+            launch_camera(jobs, n_jobs, c, cur, ctx->L.as<float4>(), ctx->stream);
+        }
+        for (int depth = 0; depth < b.levels; ++depth) {
+            nxt.count = cnt + depth + 1;
+            sh.count = cnt + (b.levels + 1) + depth;
+            TraverseCfg trace_cfg = ctx->traverse, shadow_cfg = ctx->traverse;
+            trace_cfg.work = cnt + 2 * (b.levels + 1) + depth;
+            shadow_cfg.work = cnt + 3 * (b.levels + 1) + depth;
+            {
+                KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
+                launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_paths, fast, trace_cfg, ctx->stream);
+            }
+            {
+                KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
+                launch_shade(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts,
+                             c.n_paths, ctx->stream);
+            }
+            {
+                KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
+                launch_shadow(single, jobs, sh, ctx->L.as<float4>(), c.n_paths, shadow_cfg, ctx->stream);
+            }
+            std::swap(cur, nxt);
+        }
+        {
+            KernelTimer kt(ctx, TURNER_KERNEL_RESOLVE);
+            if (acc) launch_accumulate(jobs, n_jobs, c, ctx->L.as<float4>(), acc, ctx->stream);
+            else launch_resolve(jobs, n_jobs, c, ctx->L.as<float4>(), ctx->stream);
+        }
+        TURNER_CK(cudaGetLastError());
+    }
+    return TURNER_OK;
+}
+
+// Runs a planned batch: uploads the job table, launches (through a CUDA graph
+// for multi-job batches), synchronizes and fills per-job statistics.
+int run_batch(turner_ctx* ctx, const Batch& b, double4* acc, turner_stats* stats, bool use_graph) {
+    int st = ensure_workspace(ctx, b);
+    if (st != TURNER_OK) return st;
+    TURNER_CK(cudaMemcpyAsync(ctx->jobtab.p, b.table.data(), sizeof(JobDesc) * b.table.size(),
+                              cudaMemcpyHostToDevice, ctx->stream));
+    TURNER_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (use_graph) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        const bool prof = ctx->profiling;
+        ctx->profiling = false;   // no per-kernel event pairs inside a captured graph
+        TURNER_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        st = launch_batch(ctx, b, acc);
+        const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
+        ctx->profiling = prof;
+        if (st != TURNER_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        TURNER_CK(ec);
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, ctx->stream);
+        ctx->graph_launches += e == cudaSuccess ? 1 : 0;
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        TURNER_CK(e);
+    } else {
+        st = launch_batch(ctx, b, acc);
+        if (st != TURNER_OK) return st;
+    }
+    TURNER_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    std::vector<unsigned long long> counts(2 * b.table.size());
+    TURNER_CK(cudaMemcpyAsync(counts.data(), ctx->jobcnt.p, sizeof(unsigned long long) * counts.size(),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+    TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    collect_kernel_times(ctx);
+    if (stats) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        for (size_t j = 0; j < b.table.size(); ++j) {
+            const JobDesc& d = b.table[j];
+            stats[j].rays = counts[2 * j];
+            stats[j].shadow_rays = counts[2 * j + 1];
+            stats[j].primary_rays = uint64_t(d.width) * d.height * d.spp;
+            stats[j].device_ms = ms;
+        }
+    }
+    return TURNER_OK;
+}
+
+} // namespace
+
+extern "C" {
+
 int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float* const* out_rgba,
                   turner_stats* stats, uint32_t flags) {
     if (!ctx || !jobs || !out_rgba || n_jobs == 0 || flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
+    if (n_jobs > TURNER_MAX_JOBS) return TURNER_ERR_TOO_LARGE;
     for (uint32_t j = 0; j < n_jobs; ++j) {
         if (!out_rgba[j]) return TURNER_ERR_INVALID_ARG;
         const int st = check_job(ctx, jobs[j]);
         if (st != TURNER_OK) return st;
     }
     TURNER_CK(cudaSetDevice(ctx->device));
-
-    for (uint32_t j = 0; j < n_jobs; ++j) {
-        const turner_job& job = jobs[j];
-        JobDev jd;
-        fill_job(job, ctx->scenes[job.scene_id]->view, jd);
-        const uint64_t n_pixels = uint64_t(job.width) * job.height;
-        const uint32_t px_per_chunk =
-            static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(n_pixels, ctx->chunk_paths / job.pixel_samples)));
-        const uint32_t cap = px_per_chunk * job.pixel_samples;
-        const int levels = job.max_depth + 1;
-
-        TURNER_CK(ctx->L.ensure(sizeof(float4) * cap));
-        for (int k = 0; k < 3; ++k) {
-            TURNER_CK(ctx->qa[k].ensure(sizeof(float4) * cap));
-            TURNER_CK(ctx->qb[k].ensure(sizeof(float4) * cap));
-            TURNER_CK(ctx->shq[k].ensure(sizeof(float4) * cap));
+    std::vector<float4*> outs(n_jobs);
+    uint64_t total = 0;
+    for (uint32_t j = 0; j < n_jobs; ++j) total += uint64_t(jobs[j].width) * jobs[j].height;
+    if (flags == TURNER_HOST_BUFFERS) {
+        TURNER_CK(ctx->image.ensure(sizeof(float4) * total));
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < n_jobs; ++j) {
+            outs[j] = ctx->image.as<float4>() + off;
+            off += uint64_t(jobs[j].width) * jobs[j].height;
         }
-        TURNER_CK(ctx->qa[3].ensure(sizeof(uint2) * cap));
-        TURNER_CK(ctx->qb[3].ensure(sizeof(uint2) * cap));
-        TURNER_CK(ctx->hits.ensure(sizeof(Hit) * cap));
-        const uint64_t n_chunks = (n_pixels + px_per_chunk - 1) / px_per_chunk;
-        // per chunk: [queued rays | shadow rays | trace work | shadow work], levels + 1 slots each
-        const size_t stride = 4 * size_t(levels + 1);
-        TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * stride * n_chunks));
-        float4* image = reinterpret_cast<float4*>(out_rgba[j]);
-        if (flags == TURNER_HOST_BUFFERS) {
-            TURNER_CK(ctx->image.ensure(sizeof(float4) * n_pixels));
-            image = ctx->image.as<float4>();
+    } else {
+        for (uint32_t j = 0; j < n_jobs; ++j) outs[j] = reinterpret_cast<float4*>(out_rgba[j]);
+    }
+    Batch b;
+    int st = plan_batch(ctx, jobs, n_jobs, outs.data(), true, b);
+    if (st != TURNER_OK) return st;
+    for (uint32_t j = 0; j < n_jobs; ++j) b.table[j].tone_map = jobs[j].linear_output ? 0 : 1;
+    st = run_batch(ctx, b, nullptr, stats, n_jobs > 1 || ctx->use_graph);
+    if (st != TURNER_OK) return st;
+    if (flags == TURNER_HOST_BUFFERS) {
+        for (uint32_t j = 0; j < n_jobs; ++j) {
+            TURNER_CK(cudaMemcpyAsync(out_rgba[j], outs[j], sizeof(float4) * jobs[j].width * jobs[j].height,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
         }
-        uint32_t* counters = ctx->counters.as<uint32_t>();
-        TURNER_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * stride * n_chunks, ctx->stream));
-        TURNER_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-
-        RayQueue qa{ctx->qa[0].as<float4>(), ctx->qa[1].as<float4>(), ctx->qa[2].as<float4>(), ctx->qa[3].as<uint2>(),
-                    nullptr};
-        RayQueue qb{ctx->qb[0].as<float4>(), ctx->qb[1].as<float4>(), ctx->qb[2].as<float4>(), ctx->qb[3].as<uint2>(),
-                    nullptr};
-        ShadowQueue sh{ctx->shq[0].as<float4>(), ctx->shq[1].as<float4>(), ctx->shq[2].as<float4>(), nullptr};
-        for (uint64_t c = 0; c < n_chunks; ++c) {
-            const uint32_t first = static_cast<uint32_t>(c * px_per_chunk);
-            const uint32_t npx = static_cast<uint32_t>(std::min<uint64_t>(px_per_chunk, n_pixels - first));
-            const uint32_t n_paths = npx * job.pixel_samples;
-            uint32_t* cnt = counters + stride * c;
-            RayQueue cur = qa, nxt = qb;
-            cur.count = cnt;
-            {
-                KernelTimer kt(ctx, TURNER_KERNEL_CAMERA);
-                launch_camera(jd, first, n_paths, cur, ctx->L.as<float4>(), ctx->stream);
-            }
-            for (int depth = 0; depth <= job.max_depth; ++depth) {
-                nxt.count = cnt + depth + 1;
-                sh.count = cnt + (levels + 1) + depth;
-                TraverseCfg trace_cfg = ctx->traverse, shadow_cfg = ctx->traverse;
-                trace_cfg.work = cnt + 2 * (levels + 1) + depth;
-                shadow_cfg.work = cnt + 3 * (levels + 1) + depth;
-                {
-                    KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
-                    launch_trace(jd.sc, cur, ctx->hits.as<Hit>(), n_paths, job.traversal == TURNER_TRAVERSAL_FAST,
-                                 trace_cfg, ctx->stream);
-                }
-                {
-                    KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
-                    launch_shade(jd, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), n_paths,
-                                 ctx->stream);
-                }
-                {
-                    KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
-                    launch_shadow(jd.sc, sh, ctx->L.as<float4>(), n_paths, shadow_cfg, ctx->stream);
-                }
-                std::swap(cur, nxt);
-            }
-            {
-                KernelTimer kt(ctx, TURNER_KERNEL_RESOLVE);
-                launch_resolve(jd, first, npx, ctx->L.as<float4>(), image, ctx->stream);
-            }
-            TURNER_CK(cudaGetLastError());
-        }
-        TURNER_CK(cudaEventRecord(ctx->ev1, ctx->stream));
-        if (flags == TURNER_HOST_BUFFERS) {
-            TURNER_CK(cudaMemcpyAsync(out_rgba[j], image, sizeof(float4) * n_pixels, cudaMemcpyDeviceToHost,
-                                      ctx->stream));
-        }
-        std::vector<uint32_t> host_cnt(stride * n_chunks);
-        TURNER_CK(cudaMemcpyAsync(host_cnt.data(), counters, sizeof(uint32_t) * host_cnt.size(),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
         TURNER_CK(cudaStreamSynchronize(ctx->stream));
-        collect_kernel_times(ctx);
-        if (stats) {
-            turner_stats& st = stats[j];
-            st.rays = st.primary_rays = st.shadow_rays = 0;
-            for (uint64_t c = 0; c < n_chunks; ++c) {
-                const uint32_t* cc = host_cnt.data() + stride * c;
-                st.primary_rays += cc[0];
-                for (int k = 0; k < levels; ++k) {
-                    st.rays += cc[k];
-                    st.shadow_rays += cc[levels + 1 + k];
-                }
-            }
-            float ms = 0;
-            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-            st.device_ms = ms;
-        }
     }
     return TURNER_OK;
 }
+
+int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t passes, double* out_rgba_mean,
+                             uint64_t* total_samples, uint32_t flags) {
+    if (!ctx || !job || !out_rgba_mean || flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
+    int st = check_job(ctx, *job);
+    if (st != TURNER_OK) return st;
+    TURNER_CK(cudaSetDevice(ctx->device));
+    const uint64_t n = uint64_t(job->width) * job->height;
+    // the running sum is keyed by what the image depends on; anything else resets it
+    const uint64_t key[6] = {job->scene_id, job->width, job->height, job->seed,
+                             uint64_t(uint32_t(job->max_depth)) << 32 | uint32_t(job->sampling),
+                             uint64_t(uint32_t(job->monte_carlo_samples))};
+    if (std::memcmp(key, ctx->acc_key, sizeof(key)) != 0 || ctx->acc_samples == 0) {
+        TURNER_CK(ctx->acc.ensure(sizeof(double4) * n));
+        TURNER_CK(cudaMemsetAsync(ctx->acc.p, 0, sizeof(double4) * n, ctx->stream));
+        std::memcpy(ctx->acc_key, key, sizeof(key));
+        ctx->acc_samples = 0;
+        ctx->acc_passes = 0;
+    }
+    for (uint32_t p = 0; p < passes; ++p) {
+        turner_job jp = *job;
+        // each pass draws fresh streams: a distinct seed base per pass
+        jp.seed = job->seed ^ (0x9E3779B97F4A7C15ULL * (ctx->acc_passes + 1));
+        Batch b;
+        st = plan_batch(ctx, &jp, 1, nullptr, false, b);
+        if (st != TURNER_OK) return st;
+        st = run_batch(ctx, b, ctx->acc.as<double4>(), nullptr, ctx->use_graph);
+        if (st != TURNER_OK) return st;
+        ctx->acc_passes += 1;
+        ctx->acc_samples += job->pixel_samples;
+    }
+    std::vector<double> sums(4 * n);
+    TURNER_CK(cudaMemcpyAsync(sums.data(), ctx->acc.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    const double inv = ctx->acc_samples ? 1.0 / static_cast<double>(ctx->acc_samples) : 0.0;
+    for (double& v : sums) v *= inv;
+    if (flags == TURNER_HOST_BUFFERS) {
+        std::memcpy(out_rgba_mean, sums.data(), sizeof(double) * sums.size());
+    } else {
+        TURNER_CK(cudaMemcpyAsync(out_rgba_mean, sums.data(), sizeof(double) * sums.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+        TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (total_samples) *total_samples = ctx->acc_samples;
+    return TURNER_OK;
+}
+
+int turner_set_graph_mode(turner_ctx* ctx, int always) {
+    if (!ctx) return TURNER_ERR_INVALID_ARG;
+    ctx->use_graph = always != 0;
+    return TURNER_OK;
+}
+
+uint64_t turner_graph_launch_count(turner_ctx* ctx) { return ctx ? ctx->graph_launches : 0; }
 
 int turner_set_profiling(turner_ctx* ctx, int on) {
     if (!ctx) return TURNER_ERR_INVALID_ARG;
@@ -619,8 +795,5 @@ int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox
     return TURNER_OK;
 }
 
-int turner_render_accumulate(turner_ctx*, const turner_job*, uint32_t, double*, uint64_t*, uint32_t) {
-    return TURNER_ERR_UNSUPPORTED;
-}
 
 } // extern "C"

@@ -64,6 +64,45 @@ __device__ __forceinline__ bool triangle_test(const float4* __restrict__ tri, ui
     return true;
 }
 
+// triangle_test restricted to candidates that can change a traversal's
+// answer: a valid intersection with r < bound (closest hit, bound = best r
+// so far) or r <= bound (any hit, bound = distance to the light). Skipping
+// the others is exact: the reference records a hit only if r < min_r
+// (strict, lib/kdtree.cpp:568-574) and the shadow test only asks whether some
+// valid r <= dist exists. NaN r never satisfies either comparison.
+//   - r < 0 is decided from the signs of nom and denom when nom/denom cannot
+//     underflow to -0 (|nom| > |denom| * 2^-100), without dividing;
+//   - s and t (two divides, the second 32-byte half of the record) are only
+//     computed for r inside the bound.
+template <bool INCLUSIVE>
+__device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__ tri, uint32_t id, float3 o, float3 d,
+                                                      float bound, float& r, float& s, float& t) {
+    const float4 a = __ldg(tri + 4 * size_t(id) + 0);   // v0, uv
+    const float4 n = __ldg(tri + 4 * size_t(id) + 1);   // normal, vv
+    const float denom = n.x * d.x + n.y * d.y + n.z * d.z;
+    if (denom == 0.f) return false;
+    const float nom = n.x * (a.x - o.x) + n.y * (a.y - o.y) + n.z * (a.z - o.z);
+    if (((__float_as_uint(nom) ^ __float_as_uint(denom)) & 0x80000000u) &&
+        fabsf(nom) > fabsf(denom) * 7.8886090522101181e-31f) {
+        return false;                                    // r < 0
+    }
+    r = nom / denom;
+    if (INCLUSIVE ? !(r <= bound) : !(r < bound)) return false;
+    if (r < 0) return false;
+    const float4 u = __ldg(tri + 4 * size_t(id) + 2);   // u, uu
+    const float4 v = __ldg(tri + 4 * size_t(id) + 3);   // v, denom
+    const float wx = (o.x + r * d.x) - a.x;
+    const float wy = (o.y + r * d.y) - a.y;
+    const float wz = (o.z + r * d.z) - a.z;
+    const float wv = wx * v.x + wy * v.y + wz * v.z;
+    const float wu = wx * u.x + wy * u.y + wz * u.z;
+    s = (a.w * wv - n.w * wu) / v.w;
+    if (s < 0) return false;
+    t = (a.w * wu - u.w * wv) / v.w;
+    if (t < 0 || 1 < s + t) return false;
+    return true;
+}
+
 __device__ __forceinline__ float pick(float3 v, uint32_t ax) { return ax == 0 ? v.x : (ax == 1 ? v.y : v.z); }
 
 // KDTreeIntersection::intersect (lib/kdtree.cpp:516-607).
@@ -170,6 +209,8 @@ __device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d,
 // and arithmetic, split into rounds so that a lane can take a new ray as soon
 // as its current one is finished (ray replacement, Aila & Laine 2009).
 struct TravState {
+    const uint2* nodes;
+    const float4* tri;
     float3 o, d, inv;
     uint32_t neg;    // bit ax: fixed direction component <= 0 (near child is the right one)
     uint32_t node;
@@ -180,6 +221,8 @@ struct TravState {
 
 // fix_direction + root box test. false: the ray misses the scene box.
 __device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3 d, TravState& s) {
+    s.nodes = sc.nodes;
+    s.tri = sc.tri;
     s.best = Hit{kMiss, kFltMax, 0.f, 0.f};
     const float3 fd = make_float3(d.x == 0.f ? kEps : d.x, d.y == 0.f ? kEps : d.y, d.z == 0.f ? kEps : d.z);
     s.o = o;
@@ -205,9 +248,9 @@ __device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3
 // One round: descend from s.node to a leaf, test its run, pop the next cell.
 // Returns true when the ray is finished (s.best holds the answer).
 template <bool ANY, bool FAST_EXIT>
-__device__ __forceinline__ bool trav_round(const SceneView& sc, TravState& s, float tmax, uint32_t* st_node,
-                                           float* st_enter, float* st_exit) {
-    const uint2* __restrict__ nodes = sc.nodes;
+__device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* st_node, float* st_enter,
+                                           float* st_exit) {
+    const uint2* __restrict__ nodes = s.nodes;
     uint32_t node = s.node;
     float tenter = s.tenter, texit = s.texit;
     int sp = s.sp;
@@ -237,27 +280,15 @@ __device__ __forceinline__ bool trav_round(const SceneView& sc, TravState& s, fl
     }
     for (;;) {
         float r, u, v;
-        if (triangle_test(sc.tri, w.y, s.o, s.d, r, u, v)) {
-            if (ANY) {
-                if (r <= tmax) {
-                    s.best = Hit{w.y, r, u, v};
-                    return true;
-                }
-            } else if (r < s.best.r) {
-                s.best = Hit{w.y, r, u, v};
-            }
+        if (triangle_test_bounded<ANY>(s.tri, w.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+            s.best = Hit{w.y, r, u, v};
+            if (ANY) return true;
         }
         if (w.x == 0xFFFFFFFFu) break;
         const uint32_t id2 = w.x >> 2;
-        if (triangle_test(sc.tri, id2, s.o, s.d, r, u, v)) {
-            if (ANY) {
-                if (r <= tmax) {
-                    s.best = Hit{id2, r, u, v};
-                    return true;
-                }
-            } else if (r < s.best.r) {
-                s.best = Hit{id2, r, u, v};
-            }
+        if (triangle_test_bounded<ANY>(s.tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+            s.best = Hit{id2, r, u, v};
+            if (ANY) return true;
         }
         ++node;
         w = __ldg(nodes + node);

@@ -11,23 +11,24 @@ namespace turner {
 
 // SoA ray queue (one entry per live path at one depth).
 struct RayQueue {
-    float4* o;        // origin xyz, path index (uint bits) in w
-    float4* d;        // direction xyz
+    float4* o;        // origin xyz, chunk-local path index (uint bits) in w
+    float4* d;        // direction xyz, job index (uint bits) in w
     float4* T;        // path throughput (RGBA)
     uint2* rng;       // bounce stream state
     uint32_t* count;  // number of valid entries (device)
 };
 
-// Shadow-ray queue: one entry per hit with a light in front of the surface.
+// Shadow-ray queue: one entry per hit with the light in front of the surface.
 struct ShadowQueue {
-    float4* o;        // offset hit point p2, path index in w
+    float4* o;        // offset hit point p2, chunk-local path index in w
     float4* d;        // unit light direction, distance to the light in w
     float4* c;        // contribution added to the path if the light is visible
+    uint32_t* job;    // job index
     uint32_t* count;
 };
 
-// Everything a render pass needs about one job, by value in kernel params.
-struct JobDev {
+// One image of a batch, resident in device memory (the job table).
+struct JobDesc {
     SceneView sc;
     float cam_pos[3];
     float trafo[9];
@@ -42,6 +43,16 @@ struct JobDev {
     int32_t sampling, traversal;
     float exposure, inv_gamma;
     int32_t gamma, tone_map;
+    uint64_t pixel_offset;   // first pixel of this job in the batch's pixel space
+    uint64_t path_offset;    // first path of this job in the batch's path space
+    float4* out;             // output image (device)
+};
+
+// A render pass: whole pixels [pixel0, pixel0 + n_pixels) of the batch's
+// pixel space, which are paths [path0, path0 + n_paths).
+struct Chunk {
+    uint64_t pixel0, path0;
+    uint32_t n_pixels, n_paths;
 };
 
 // How traversal kernels are launched. persistent: one grid of resident
@@ -56,15 +67,22 @@ struct TraverseCfg {
 void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                       const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
                       int fast, const TraverseCfg& cfg, cudaStream_t stream);
-void launch_camera(const JobDev& job, uint32_t first_pixel, uint32_t n_paths, const RayQueue& q, float4* L,
+
+// `single` is the scene of every job when the batch has one scene (rays then
+// skip the per-ray job-table lookup); nullptr for multi-scene batches.
+void launch_camera(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const RayQueue& q, float4* L,
                    cudaStream_t stream);
-void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast,
-                  const TraverseCfg& cfg, cudaStream_t stream);
-void launch_shade(const JobDev& job, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
-                  const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream);
-void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, const TraverseCfg& cfg,
-                   cudaStream_t stream);
-void launch_resolve(const JobDev& job, uint32_t first_pixel, uint32_t n_pixels, const float4* L, float4* out,
-                    cudaStream_t stream);
+void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& q, Hit* hits, uint32_t capacity,
+                  int fast, const TraverseCfg& cfg, cudaStream_t stream);
+// job_counts (optional): per job {traced rays, shadow rays}, 64-bit
+void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
+                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
+                  cudaStream_t stream);
+void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
+                   const TraverseCfg& cfg, cudaStream_t stream);
+void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream);
+// acc[p] += (double) sum of the chunk's sample radiance for pixel p (linear)
+void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, double4* acc,
+                       cudaStream_t stream);
 
 } // namespace turner

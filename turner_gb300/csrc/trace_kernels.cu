@@ -1,13 +1,14 @@
 // Wavefront path-tracing kernels for sm_103a (compiled with -fmad=false).
 //
-// One render pass over a chunk of whole pixels:
+// One render pass over a chunk of whole pixels of a batch of images (the job
+// table, `JobDesc`, lives in device memory):
 //   k_camera   primary rays for every (pixel, sample) path        main.cpp:200-214
-//   per depth 0..max_depth:
-//     k_trace   closest hit of every queued ray                   kdtree.cpp:516-607
+//   per depth 0..max depth of the batch:
+//     k_traverse<QueueSrc>   closest hit of every queued ray     kdtree.cpp:516-607
 //     k_shade   hit point, interpolated normal, offset, next-event
 //               shadow ray, bounce direction; appends live paths to
 //               the next queue (warp ballot + one atomic per warp)  pathtracer.cpp:14-102
-//     k_shadow  any-hit occlusion test; adds the direct term       pathtracer.cpp:44-58
+//     k_traverse<ShadowSrc>  any-hit occlusion; adds the direct term   pathtracer.cpp:44-58
 //   k_resolve  per-pixel mean over samples in sample order, then exposure and
 //              gamma                                              main.cpp:216-223
 // The radiance of a path is accumulated forward: L += T * diffuse *
@@ -15,6 +16,8 @@
 // miss, with T *= diffuse * 2 cos(theta) per uniform bounce (diffuse for a
 // cosine bounce). This is the reference's recursion
 // L_k = diffuse * (direct / pi + 2 cos L_{k+1}) unrolled.
+#include <algorithm>
+
 #include "device.cuh"
 #include "kernels.h"
 
@@ -38,6 +41,27 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
     return base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
 }
 
+// Job owning global path g / global pixel p (job offsets ascend).
+__device__ __forceinline__ uint32_t job_of_path(const JobDesc* jobs, uint32_t n_jobs, uint64_t g) {
+    uint32_t lo = 0, hi = n_jobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].path_offset <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t job_of_pixel(const JobDesc* jobs, uint32_t n_jobs, uint64_t p) {
+    uint32_t lo = 0, hi = n_jobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].pixel_offset <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(kBlock) k_intersect(SceneView sc, const float* __restrict__ ox,
                                                       const float* __restrict__ oy, const float* __restrict__ oz,
                                                       const float* __restrict__ dx, const float* __restrict__ dy,
@@ -57,17 +81,21 @@ __global__ void __launch_bounds__(kBlock) k_intersect(SceneView sc, const float*
 
 // Camera::raster2cam (lib/types.h:117-123) with jitter from the path's own
 // xorshift stream; the direction is not normalised.
-__global__ void __launch_bounds__(kBlock) k_camera(JobDev job, uint32_t first_pixel, uint32_t n_paths, RayQueue q,
-                                                   float4* __restrict__ L) {
+__global__ void __launch_bounds__(kBlock) k_camera(const JobDesc* __restrict__ jobs, uint32_t n_jobs, Chunk c,
+                                                   RayQueue q, float4* __restrict__ L) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) *q.count = n_paths;
-    if (i >= n_paths) return;
-    const uint32_t local_pixel = i / job.spp;
-    const uint32_t sample = i - local_pixel * job.spp;
-    const uint32_t pixel = first_pixel + local_pixel;
-    const uint32_t y = pixel / job.width, x = pixel - y * job.width;
+    if (i == 0) *q.count = c.n_paths;
+    if (i >= c.n_paths) return;
+    const uint64_t g = c.path0 + i;
+    const uint32_t j = job_of_path(jobs, n_jobs, g);
+    const JobDesc& job = jobs[j];
+    const uint64_t local = g - job.path_offset;
+    const uint64_t pixel = local / job.spp;
+    const uint32_t sample = static_cast<uint32_t>(local - pixel * job.spp);
+    const uint32_t y = static_cast<uint32_t>(pixel / job.width);
+    const uint32_t x = static_cast<uint32_t>(pixel - uint64_t(y) * job.width);
     uint64_t js, bs;
-    path_seeds(job.seed, uint64_t(pixel) * job.spp + sample, js, bs);
+    path_seeds(job.seed, pixel * job.spp + sample, js, bs);
     const float jx = xorshift_float(js);
     const float jy = xorshift_float(js);
     const float px = static_cast<float>(x) + jx, py = static_cast<float>(y) + jy;
@@ -79,30 +107,20 @@ __global__ void __launch_bounds__(kBlock) k_camera(JobDev job, uint32_t first_pi
     const float3 d = make_float3(m[0] * vx + m[1] * vy + m[2] * vz, m[3] * vx + m[4] * vy + m[5] * vz,
                                  m[6] * vx + m[7] * vy + m[8] * vz);
     q.o[i] = make_float4(job.cam_pos[0], job.cam_pos[1], job.cam_pos[2], __uint_as_float(i));
-    q.d[i] = make_float4(d.x, d.y, d.z, 0.f);
+    q.d[i] = make_float4(d.x, d.y, d.z, __uint_as_float(j));
     q.T[i] = make_float4(1.f, 1.f, 1.f, 1.f);
     q.rng[i] = make_uint2(static_cast<uint32_t>(bs), static_cast<uint32_t>(bs >> 32));
     L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-__global__ void __launch_bounds__(kBlock) k_trace(SceneView sc, RayQueue q, Hit* __restrict__ hits, int fast) {
-    const uint32_t n = *q.count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = q.o[i];
-        const float4 d = q.d[i];
-        const float3 o3 = make_float3(o.x, o.y, o.z), d3 = make_float3(d.x, d.y, d.z);
-        hits[i] = fast ? traverse<false, true>(sc, o3, d3, 0.f) : traverse<false, false>(sc, o3, d3, 0.f);
-    }
 }
 
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
 __device__ __forceinline__ float4 scale4(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
 __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 
-__global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueue in, const Hit* __restrict__ hits,
-                                                  RayQueue out, ShadowQueue sh, float4* __restrict__ L) {
+__global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jobs, int depth, RayQueue in,
+                                                  const Hit* __restrict__ hits, RayQueue out, ShadowQueue sh,
+                                                  float4* __restrict__ L, unsigned long long* __restrict__ job_counts) {
     const uint32_t n = *in.count;
-    const bool bounce_allowed = depth < job.max_depth && job.mc > 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     // warp-uniform loop so every lane reaches the ballots
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
@@ -111,16 +129,19 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
         bool emit_shadow = false, emit_bounce = false;
         float4 sh_o, sh_d, sh_c, b_o, b_d, b_T;
         uint2 b_rng;
+        uint32_t jidx = 0;
         if (valid) {
             const Hit h = hits[i];
             const float4 o4 = in.o[i];
+            const float4 d4 = in.d[i];
+            jidx = __float_as_uint(d4.w);
+            const JobDesc& job = jobs[jidx];
             const uint32_t path = __float_as_uint(o4.w);
             const float4 T = in.T[i];
             if (h.id >= kMiss) {
                 // miss: trace() returns conf.bg_color (alpha 1)
                 L[path] = add4(L[path], mul4(T, make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f)));
             } else {
-                const float4 d4 = in.d[i];
                 const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
                 const float4* rec = job.sc.shade + 4 * size_t(h.id);
                 const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2), s3 = __ldg(rec + 3);
@@ -151,7 +172,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
                         emit_shadow = true;
                     }
                 }
-                if (bounce_allowed) {
+                if (depth < job.max_depth && job.mc > 0) {
                     float m[9];
                     from_to_z(nrm, m);
                     const uint2 r2 = in.rng[i];
@@ -178,11 +199,21 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
                     const float3 dir = make_float3(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
                                                    m[6] * x + m[7] * y + m[8] * z);
                     b_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
-                    b_d = make_float4(dir.x, dir.y, dir.z, 0.f);
+                    b_d = make_float4(dir.x, dir.y, dir.z, __uint_as_float(jidx));
                     b_T = scale4(weight, Td);
                     b_rng = make_uint2(static_cast<uint32_t>(rs), static_cast<uint32_t>(rs >> 32));
                     emit_bounce = true;
                 }
+            }
+        }
+        // per-job statistics: this queue entry is one traced ray of job jidx
+        // (pathtracer.cpp:21); lanes of the same job add with one atomic
+        if (job_counts) {
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, valid ? jidx : 0xFFFFFFFFu);
+            const unsigned shadow_peers = __ballot_sync(0xFFFFFFFFu, emit_shadow) & peers;
+            if (valid && static_cast<int>(lane_id()) == __ffs(peers) - 1) {
+                atomicAdd(job_counts + 2 * jidx, static_cast<unsigned long long>(__popc(peers)));
+                if (shadow_peers) atomicAdd(job_counts + 2 * jidx + 1, static_cast<unsigned long long>(__popc(shadow_peers)));
             }
         }
         const uint32_t si = warp_append(sh.count, emit_shadow);
@@ -190,6 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
             sh.o[si] = sh_o;
             sh.d[si] = sh_d;
             sh.c[si] = sh_c;
+            sh.job[si] = jidx;
         }
         const uint32_t bi = warp_append(out.count, emit_bounce);
         if (emit_bounce) {
@@ -202,19 +234,20 @@ __global__ void __launch_bounds__(kBlock) k_shade(JobDev job, int depth, RayQueu
 }
 
 // ---------------------------------------------------------------- persistent
-// Ray sources for the persistent traversal kernel: where rays come from and
-// where the answer goes.
+// Ray sources for the persistent traversal kernel: where rays come from, which
+// scene they are traced in, and where the answer goes.
 struct QueueSrc {           // closest hit of a ray queue -> hit array
     const float4* o;
     const float4* d;
     const uint32_t* cnt;
     Hit* hits;
     __device__ uint32_t count() const { return *cnt; }
-    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax, uint32_t& job) const {
         const float4 a = o[i], b = d[i];
         o3 = make_float3(a.x, a.y, a.z);
         d3 = make_float3(b.x, b.y, b.z);
         tmax = 0.f;
+        job = __float_as_uint(b.w);
     }
     __device__ void store(uint32_t i, const Hit& h) const { hits[i] = h; }
 };
@@ -223,14 +256,16 @@ struct ShadowSrc {          // any hit of a shadow queue -> direct light if unbl
     const float4* o;
     const float4* d;
     const float4* c;
+    const uint32_t* jobs;
     const uint32_t* cnt;
     float4* L;
     __device__ uint32_t count() const { return *cnt; }
-    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax, uint32_t& job) const {
         const float4 a = o[i], b = d[i];
         o3 = make_float3(a.x, a.y, a.z);
         d3 = make_float3(b.x, b.y, b.z);
         tmax = b.w;
+        job = jobs[i];
     }
     __device__ void store(uint32_t i, const Hit& h) const {
         if (h.id >= kMiss) {
@@ -248,10 +283,11 @@ struct SoaSrc {             // turner_intersect batches
     uint32_t* id;
     float *r, *s, *t;
     __device__ uint32_t count() const { return n; }
-    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax) const {
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax, uint32_t& job) const {
         o3 = make_float3(ox[i], oy[i], oz[i]);
         d3 = make_float3(dx[i], dy[i], dz[i]);
         tmax = 0.f;
+        job = 0;
     }
     __device__ void store(uint32_t i, const Hit& h) const {
         const bool hit = h.id < kMiss;
@@ -264,9 +300,11 @@ struct SoaSrc {             // turner_intersect batches
 
 // Persistent traversal: each lane holds one ray; lanes whose ray is finished
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
-// while rays of very different lengths are traversed.
-template <class Src, bool ANY, bool FAST>
-__global__ void __launch_bounds__(kBlock) k_traverse(SceneView sc, Src src, uint32_t* __restrict__ work) {
+// while rays of very different lengths are traversed. MULTI: every ray names
+// its job and is traced in that job's scene.
+template <class Src, bool ANY, bool FAST, bool MULTI>
+__global__ void __launch_bounds__(kBlock) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
+                                                     uint32_t* __restrict__ work) {
     const uint32_t n = src.count();
     uint32_t st_node[kStackCap];
     float st_enter[kStackCap], st_exit[kStackCap];
@@ -289,8 +327,10 @@ __global__ void __launch_bounds__(kBlock) k_traverse(SceneView sc, Src src, uint
                     exhausted = true;
                 } else {
                     float3 o, d;
-                    src.load(idx, o, d, tmax);
-                    if (trav_begin(sc, o, d, s)) {
+                    uint32_t job;
+                    src.load(idx, o, d, tmax, job);
+                    const bool in_box = MULTI ? trav_begin(jobs[job].sc, o, d, s) : trav_begin(single, o, d, s);
+                    if (in_box) {
                         cur = idx;
                         active = true;
                     } else {
@@ -300,34 +340,25 @@ __global__ void __launch_bounds__(kBlock) k_traverse(SceneView sc, Src src, uint
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
-        if (active && trav_round<ANY, FAST>(sc, s, tmax, st_node, st_enter, st_exit)) {
+        if (active && trav_round<ANY, FAST>(s, tmax, st_node, st_enter, st_exit)) {
             src.store(cur, s.best);
             active = false;
         }
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_shadow(SceneView sc, ShadowQueue sh, float4* __restrict__ L) {
-    const uint32_t n = *sh.count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = sh.o[i];
-        const float4 d = sh.d[i];
-        const Hit h = traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w);
-        if (h.id >= kMiss) {
-            const uint32_t path = __float_as_uint(o.w);
-            L[path] = add4(L[path], sh.c[i]);
-        }
-    }
-}
-
 // Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
 // on RGB; alpha is kept (lib/effects.h:15-49).
-__global__ void __launch_bounds__(kBlock) k_resolve(JobDev job, uint32_t first_pixel, uint32_t n_pixels,
-                                                    const float4* __restrict__ L, float4* __restrict__ out) {
+__global__ void __launch_bounds__(kBlock) k_resolve(const JobDesc* __restrict__ jobs, uint32_t n_jobs, Chunk c,
+                                                    const float4* __restrict__ L) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_pixels) return;
+    if (i >= c.n_pixels) return;
+    const uint64_t gp = c.pixel0 + i;
+    const uint32_t j = job_of_pixel(jobs, n_jobs, gp);
+    const JobDesc& job = jobs[j];
+    const uint64_t local = gp - job.pixel_offset;
+    const float4* l = L + (job.path_offset + local * job.spp - c.path0);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4* l = L + size_t(i) * job.spp;
     for (uint32_t k = 0; k < job.spp; ++k) acc = add4(acc, l[k]);
     const float fs = static_cast<float>(job.spp);
     acc = make_float4(acc.x / fs, acc.y / fs, acc.z / fs, acc.w / fs);
@@ -341,7 +372,28 @@ __global__ void __launch_bounds__(kBlock) k_resolve(JobDev job, uint32_t first_p
             acc.z = powf(acc.z, job.inv_gamma);
         }
     }
-    out[first_pixel + i] = acc;
+    job.out[local] = acc;
+}
+
+// FP64 running sums of linear radiance for converged reference images.
+__global__ void __launch_bounds__(kBlock) k_accumulate(const JobDesc* __restrict__ jobs, uint32_t n_jobs, Chunk c,
+                                                       const float4* __restrict__ L, double4* __restrict__ acc) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n_pixels) return;
+    const uint64_t gp = c.pixel0 + i;
+    const uint32_t j = job_of_pixel(jobs, n_jobs, gp);
+    const JobDesc& job = jobs[j];
+    const uint64_t local = gp - job.pixel_offset;
+    const float4* l = L + (job.path_offset + local * job.spp - c.path0);
+    double4 a = acc[gp];
+    for (uint32_t k = 0; k < job.spp; ++k) {
+        const float4 v = l[k];
+        a.x += v.x;
+        a.y += v.y;
+        a.z += v.z;
+        a.w += v.w;
+    }
+    acc[gp] = a;
 }
 
 inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
@@ -361,12 +413,40 @@ template <class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap
     return static_cast<unsigned>(sms) * per;
 }
 
-template <class Src, bool ANY, bool FAST>
-void run_traverse(const SceneView& sc, const Src& src, uint32_t capacity, const TraverseCfg& cfg,
-                  cudaStream_t stream) {
-    auto kernel = k_traverse<Src, ANY, FAST>;
+template <class Src, bool ANY, bool FAST, bool MULTI>
+void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
+                  const TraverseCfg& cfg, cudaStream_t stream) {
+    auto kernel = k_traverse<Src, ANY, FAST, MULTI>;
     const unsigned grid = std::min(persistent_grid(kernel, cfg.blocks_per_sm), std::max(1u, grid_for(capacity)));
-    kernel<<<grid, kBlock, 0, stream>>>(sc, src, cfg.work);
+    kernel<<<grid, kBlock, 0, stream>>>(single, jobs, src, cfg.work);
+}
+
+// One thread per queue slot (the non-persistent launch shape).
+template <bool FAST>
+__global__ void __launch_bounds__(kBlock) k_trace_flat(SceneView single, const JobDesc* __restrict__ jobs, bool multi,
+                                                       RayQueue q, Hit* __restrict__ hits) {
+    const uint32_t n = *q.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = q.o[i];
+        const float4 d = q.d[i];
+        const SceneView& sc = multi ? jobs[__float_as_uint(d.w)].sc : single;
+        hits[i] = traverse<false, FAST>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_shadow_flat(SceneView single, const JobDesc* __restrict__ jobs, bool multi,
+                                                        ShadowQueue sh, float4* __restrict__ L) {
+    const uint32_t n = *sh.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = sh.o[i];
+        const float4 d = sh.d[i];
+        const SceneView& sc = multi ? jobs[sh.job[i]].sc : single;
+        const Hit h = traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w);
+        if (h.id >= kMiss) {
+            const uint32_t path = __float_as_uint(o.w);
+            L[path] = add4(L[path], sh.c[i]);
+        }
+    }
 }
 
 } // namespace
@@ -377,47 +457,61 @@ void launch_intersect(const SceneView& sc, const float* ox, const float* oy, con
     if (n == 0) return;
     if (cfg.persistent && n < (1ull << 31)) {
         const SoaSrc src{ox, oy, oz, dx, dy, dz, static_cast<uint32_t>(n), id, r, s, t};
-        if (fast) run_traverse<SoaSrc, false, true>(sc, src, static_cast<uint32_t>(n), cfg, stream);
-        else run_traverse<SoaSrc, false, false>(sc, src, static_cast<uint32_t>(n), cfg, stream);
+        if (fast) run_traverse<SoaSrc, false, true, false>(sc, nullptr, src, static_cast<uint32_t>(n), cfg, stream);
+        else run_traverse<SoaSrc, false, false, false>(sc, nullptr, src, static_cast<uint32_t>(n), cfg, stream);
         return;
     }
     k_intersect<<<grid_for(n), kBlock, 0, stream>>>(sc, ox, oy, oz, dx, dy, dz, n, id, r, s, t, fast);
 }
 
-void launch_camera(const JobDev& job, uint32_t first_pixel, uint32_t n_paths, const RayQueue& q, float4* L,
+void launch_camera(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const RayQueue& q, float4* L,
                    cudaStream_t stream) {
-    k_camera<<<grid_for(n_paths), kBlock, 0, stream>>>(job, first_pixel, n_paths, q, L);
+    k_camera<<<grid_for(c.n_paths), kBlock, 0, stream>>>(jobs, n_jobs, c, q, L);
 }
 
-void launch_trace(const SceneView& sc, const RayQueue& q, Hit* hits, uint32_t capacity, int fast,
-                  const TraverseCfg& cfg, cudaStream_t stream) {
+void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& q, Hit* hits, uint32_t capacity,
+                  int fast, const TraverseCfg& cfg, cudaStream_t stream) {
+    const SceneView sv = single ? *single : SceneView{};
     if (cfg.persistent) {
         const QueueSrc src{q.o, q.d, q.count, hits};
-        if (fast) run_traverse<QueueSrc, false, true>(sc, src, capacity, cfg, stream);
-        else run_traverse<QueueSrc, false, false>(sc, src, capacity, cfg, stream);
+        if (single) {
+            if (fast) run_traverse<QueueSrc, false, true, false>(sv, jobs, src, capacity, cfg, stream);
+            else run_traverse<QueueSrc, false, false, false>(sv, jobs, src, capacity, cfg, stream);
+        } else {
+            if (fast) run_traverse<QueueSrc, false, true, true>(sv, jobs, src, capacity, cfg, stream);
+            else run_traverse<QueueSrc, false, false, true>(sv, jobs, src, capacity, cfg, stream);
+        }
         return;
     }
-    k_trace<<<grid_for(capacity), kBlock, 0, stream>>>(sc, q, hits, fast);
+    if (fast) k_trace_flat<true><<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, q, hits);
+    else k_trace_flat<false><<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, q, hits);
 }
 
-void launch_shade(const JobDev& job, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
-                  const ShadowQueue& sh, float4* L, uint32_t capacity, cudaStream_t stream) {
-    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(job, depth, in, hits, out, sh, L);
+void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
+                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
+                  cudaStream_t stream) {
+    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts);
 }
 
-void launch_shadow(const SceneView& sc, const ShadowQueue& sh, float4* L, uint32_t capacity, const TraverseCfg& cfg,
-                   cudaStream_t stream) {
+void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
+                   const TraverseCfg& cfg, cudaStream_t stream) {
+    const SceneView sv = single ? *single : SceneView{};
     if (cfg.persistent) {
-        const ShadowSrc src{sh.o, sh.d, sh.c, sh.count, L};
-        run_traverse<ShadowSrc, true, false>(sc, src, capacity, cfg, stream);
+        const ShadowSrc src{sh.o, sh.d, sh.c, sh.job, sh.count, L};
+        if (single) run_traverse<ShadowSrc, true, false, false>(sv, jobs, src, capacity, cfg, stream);
+        else run_traverse<ShadowSrc, true, false, true>(sv, jobs, src, capacity, cfg, stream);
         return;
     }
-    k_shadow<<<grid_for(capacity), kBlock, 0, stream>>>(sc, sh, L);
+    k_shadow_flat<<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, sh, L);
 }
 
-void launch_resolve(const JobDev& job, uint32_t first_pixel, uint32_t n_pixels, const float4* L, float4* out,
-                    cudaStream_t stream) {
-    k_resolve<<<grid_for(n_pixels), kBlock, 0, stream>>>(job, first_pixel, n_pixels, L, out);
+void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream) {
+    k_resolve<<<grid_for(c.n_pixels), kBlock, 0, stream>>>(jobs, n_jobs, c, L);
+}
+
+void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, double4* acc,
+                       cudaStream_t stream) {
+    k_accumulate<<<grid_for(c.n_pixels), kBlock, 0, stream>>>(jobs, n_jobs, c, L, acc);
 }
 
 } // namespace turner
