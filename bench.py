@@ -168,6 +168,60 @@ def run_reference(args) -> None:
     }))
 
 
+def run_batch64(args) -> None:
+    """The batched workload: 64 independent scenes in one launch sequence.
+
+    Each scene is a seeded clustered triangle soup in the room, triangle count
+    log-uniform in [1k, max], image side uniform in [128, 1024], pixel samples
+    from {1, 4, 16, 64}, max depth 1-5, its own streams. Reports Mrays/s over
+    the whole batch (one CUDA graph launch per step); not the headline line."""
+    import torch
+
+    import turner_gb300 as tg
+
+    rng = np.random.default_rng(2026)
+    n = args.batch_scenes
+    counts = np.exp(rng.uniform(np.log(1000), np.log(args.batch_max_tris), n)).astype(int)
+    sides = rng.integers(128, 1025, n)
+    spps = rng.choice([1, 4, 16, 64], n)
+    depths = rng.integers(1, 6, n)
+    ctx = tg.Context(0)
+    t0 = time.perf_counter()
+    jobs, tris = [], 0
+    for k in range(n):
+        m = tg.make_scene(tg.SCENE_SOUP, count=int(counts[k]), seed=1000 + k)
+        tree = tg.KDTree.from_mesh(m)
+        sid = ctx.upload_tree(tree)
+        tris += m.n_triangles
+        jobs.append(tg.make_job(sid, m, int(sides[k]), int(sides[k]), pixel_samples=int(spps[k]),
+                                max_depth=int(depths[k]), seed=77 + k))
+    build_s = time.perf_counter() - t0
+    tuning = ctx.autotune(jobs, force=True).as_dict() if args.autotune else ctx.get_tuning().as_dict()
+    outs = [torch.empty((j.height, j.width, 4), dtype=torch.float32, device="cuda") for j in jobs]
+    ptrs = [o.data_ptr() for o in outs]
+    for _ in range(args.warmup):
+        ctx.render(jobs, ptrs, tg.DEVICE_BUFFERS)
+    torch.cuda.synchronize()
+    g0, l0 = ctx.graph_launch_count(), ctx.launch_count()
+    dev_ms, rays = 0.0, 0
+    for _ in range(args.steps):
+        _, stats = ctx.render(jobs, ptrs, tg.DEVICE_BUFFERS)
+        dev_ms += stats[0].device_ms
+        rays += sum(s.rays for s in stats)
+    torch.cuda.synchronize()
+    print(json.dumps({
+        "metric": "Mrays/s, 64-scene batch (reference ray count)", "value": round(rays / (dev_ms / 1000) / 1e6, 3),
+        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batch of {n} soups", "triangles_total": int(tris),
+                   "paths_per_step": int(sum(j.width * j.height * j.pixel_samples for j in jobs)),
+                   "rays_per_step": int(rays // args.steps), "host_tree_build_s": round(build_s, 2),
+                   "graph_launches_per_step": (ctx.graph_launch_count() - g0) / args.steps,
+                   "kernel_launches_per_step": (ctx.launch_count() - l0) / args.steps, "tuning": tuning},
+    }))
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,7 +235,14 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="480x270 frame of the same scene (for profiler captures; not a bench line)")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch64"])
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-max-tris", type=int, default=500_000)
+    ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
+    if args.workload == "batch64":
+        run_batch64(args)
+        return
     if args.small:
         global WIDTH, HEIGHT, WORKLOAD
         WIDTH, HEIGHT = 480, 270

@@ -237,6 +237,30 @@ int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox
  * turner_stats per job (device_ms is the whole batch's). Synchronous. */
 int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float* const* out_rgba,
                   turner_stats* stats, uint32_t flags);
+/* Launch configuration picked by turner_autotune. No reference counterpart.
+ *   persistent     1: persistent traversal with ray replacement, 0: one thread per ray
+ *   blocks_per_sm  resident traversal blocks per SM (0 = occupancy limit)
+ *   block          threads per traversal block (128 or 256)
+ *   stack          traversal stack entries (64 or 128; 64 only if every scene fits)
+ *   chunk_paths    paths in flight per render pass (queue length) */
+typedef struct turner_tuning {
+    int32_t persistent;
+    uint32_t blocks_per_sm;
+    uint32_t block;
+    uint32_t stack;
+    uint32_t chunk_paths;
+    double ms;             /* device time of the batch with this configuration */
+    uint32_t candidates;   /* configurations timed (0: taken from the cache)  */
+} turner_tuning;
+/* Times configurations on the given batch (coordinate descent over the
+ * fields above, two renders each, CUDA events) and applies the fastest to the
+ * context. Results are cached per GPU model and batch shape in the file named
+ * by TURNER_TUNE_CACHE (default ~/.cache/turner_gb300_tuning.txt); force != 0
+ * ignores the cache. */
+int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, int force, turner_tuning* out);
+int turner_set_tuning(turner_ctx* ctx, const turner_tuning* tuning);
+int turner_get_tuning(turner_ctx* ctx, turner_tuning* tuning);
+
 /* Capture single-job renders into a CUDA graph too (always != 0). No
  * reference counterpart. */
 int turner_set_graph_mode(turner_ctx* ctx, int always);

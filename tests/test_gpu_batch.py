@@ -125,6 +125,30 @@ def test_fp64_accumulation(ctx, scenes):
     assert total_new == 4
 
 
+def test_autotune_caches_and_keeps_images(ctx, scenes, tmp_path, monkeypatch):
+    """The tuner times launch shapes on the batch, applies the fastest and
+    caches it per GPU and batch shape; any tuned shape renders the same image."""
+    monkeypatch.setenv("TURNER_TUNE_CACHE", str(tmp_path / "tuning.txt"))
+    jobs = make_jobs(scenes)[:3]
+    before, _ = ctx.render(jobs)
+    t = ctx.autotune(jobs, force=True)
+    assert t.candidates >= 5 and t.ms > 0
+    assert t.block in (128, 256) and t.stack in (64, 128) and t.chunk_paths >= 1024
+    cached = ctx.autotune(jobs)
+    assert cached.candidates == 0 and cached.as_dict()["block"] == t.block
+    after, _ = ctx.render(jobs)
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    for shape in ({"block": 256, "stack": 64}, {"block": 128, "stack": 128}):
+        tt = ctx.get_tuning()
+        tt.block, tt.stack = shape["block"], shape["stack"]
+        ctx.set_tuning(tt)
+        again, _ = ctx.render(jobs)
+        for a, b in zip(before, again):
+            assert np.array_equal(a, b)
+    ctx.set_tuning(tg.Tuning(1, 0, 128, 128, 1 << 24, 0.0, 0))
+
+
 def test_too_many_jobs_rejected(ctx, scenes):
     m, sid, _ = scenes["room"]
     with pytest.raises(tg.TurnerError) as e:

@@ -77,6 +77,14 @@ class Job(C.Structure):
                 ("linear_output", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("persistent", C.c_int32), ("blocks_per_sm", C.c_uint32), ("block", C.c_uint32),
+                ("stack", C.c_uint32), ("chunk_paths", C.c_uint32), ("ms", C.c_double), ("candidates", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Stats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("primary_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("device_ms", C.c_double)]
@@ -104,6 +112,9 @@ def _lib() -> C.CDLL:
         "turner_set_chunk_paths": (C.c_int, [_P, C.c_uint32]),
         "turner_set_profiling": (C.c_int, [_P, C.c_int]),
         "turner_set_graph_mode": (C.c_int, [_P, C.c_int]),
+        "turner_autotune": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.c_int, C.POINTER(Tuning)]),
+        "turner_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+        "turner_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
         "turner_graph_launch_count": (C.c_uint64, [_P]),
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
@@ -327,6 +338,21 @@ class Context:
         """Device-buffer batch intersect (six ray pointers, four output pointers)."""
         _check(_lib().turner_intersect(self._h, scene_id, *ptrs, n, *out_ptrs, mode, DEVICE_BUFFERS),
                "turner_intersect")
+
+    def autotune(self, jobs: list[Job], force: bool = False) -> Tuning:
+        """Times launch configurations on `jobs` and applies the fastest."""
+        arr = (Job * len(jobs))(*jobs)
+        t = Tuning()
+        _check(_lib().turner_autotune(self._h, arr, len(jobs), 1 if force else 0, C.byref(t)), "turner_autotune")
+        return t
+
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        _check(_lib().turner_get_tuning(self._h, C.byref(t)), "turner_get_tuning")
+        return t
+
+    def set_tuning(self, t: Tuning) -> None:
+        _check(_lib().turner_set_tuning(self._h, C.byref(t)), "turner_set_tuning")
 
     def set_graph_mode(self, always: bool) -> None:
         _check(_lib().turner_set_graph_mode(self._h, 1 if always else 0), "turner_set_graph_mode")

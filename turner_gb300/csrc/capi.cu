@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -59,7 +60,7 @@ struct turner_ctx {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
     // render workspace
-    DevBuf L, qa[4], qb[4], hits, shq[3], shjob, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc;
+    DevBuf L, qa[4], qb[4], hits, shq[3], shjob, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
     uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
     uint64_t acc_samples = 0, acc_passes = 0;
     bool use_graph = false;            // capture single-job renders too
@@ -366,6 +367,7 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
     const int fast = mode == TURNER_TRAVERSAL_FAST;
     TURNER_CK(ctx->work.ensure(sizeof(uint32_t) * 64));
     TraverseCfg cfg = ctx->traverse;
+    if (sc.height > 64) cfg.stack = kStackCap;
     cfg.work = ctx->work.as<uint32_t>();
     if (flags == TURNER_DEVICE_BUFFERS) {
         for (uint64_t b = 0; b < n; b += (1ull << 30)) {
@@ -438,6 +440,7 @@ struct Batch {
     int levels = 0;                  // largest max_depth + 1
     bool single_scene = true;
     SceneView single{};
+    uint32_t max_height = 0;         // deepest traversal stack any scene needs
 };
 
 int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4* const* outs, bool tone_map,
@@ -457,6 +460,7 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
         max_spp = std::max(max_spp, d.spp);
         b.levels = std::max(b.levels, d.max_depth + 1);
         if (jobs[j].scene_id != jobs[0].scene_id) b.single_scene = false;
+        b.max_height = std::max(b.max_height, d.sc.height);
     }
     b.total_pixels = pixels;
     b.single = b.table[0].sc;
@@ -533,7 +537,9 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
         for (int depth = 0; depth < b.levels; ++depth) {
             nxt.count = cnt + depth + 1;
             sh.count = cnt + (b.levels + 1) + depth;
-            TraverseCfg trace_cfg = ctx->traverse, shadow_cfg = ctx->traverse;
+            TraverseCfg trace_cfg = ctx->traverse;
+            if (b.max_height > 64) trace_cfg.stack = kStackCap;   // the short stack only where every scene fits
+            TraverseCfg shadow_cfg = trace_cfg;
             trace_cfg.work = cnt + 2 * (b.levels + 1) + depth;
             shadow_cfg.work = cnt + 3 * (b.levels + 1) + depth;
             {
@@ -700,6 +706,193 @@ int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t pa
         TURNER_CK(cudaStreamSynchronize(ctx->stream));
     }
     if (total_samples) *total_samples = ctx->acc_samples;
+    return TURNER_OK;
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------ tuning
+namespace {
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 0x100000001B3ULL;
+    return h;
+}
+
+// What a tuning result depends on: the GPU and the shape of the batch.
+std::string tuning_key(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, ctx->device);
+    uint64_t h = 0xCBF29CE484222325ULL;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const SceneView& v = ctx->scenes[jobs[j].scene_id]->view;
+        const uint64_t f[9] = {v.n_tris, v.n_nodes, v.height, jobs[j].width, jobs[j].height, jobs[j].pixel_samples,
+                               uint64_t(uint32_t(jobs[j].max_depth)), uint64_t(uint32_t(jobs[j].sampling)),
+                               uint64_t(uint32_t(jobs[j].traversal))};
+        h = fnv1a(h, f, sizeof(f));
+    }
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%016llx", static_cast<unsigned long long>(h));
+    std::string name(prop.name);
+    for (char& c : name) if (c == ' ' || c == '|') c = '_';
+    return name + "|sm" + std::to_string(prop.multiProcessorCount) + "|" + buf;
+}
+
+std::string tuning_cache_path() {
+    if (const char* p = std::getenv("TURNER_TUNE_CACHE")) return p;
+    const char* home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/turner_gb300_tuning.txt";
+}
+
+bool tuning_lookup(const std::string& key, turner_tuning& t) {
+    FILE* f = std::fopen(tuning_cache_path().c_str(), "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        char k[256];
+        turner_tuning r{};
+        if (std::sscanf(line, "%255s %d %u %u %u %u %lf", k, &r.persistent, &r.blocks_per_sm, &r.block, &r.stack,
+                        &r.chunk_paths, &r.ms) == 7 && key == k) {
+            t = r;
+            found = true;   // the last entry for a key wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+void tuning_store(const std::string& key, const turner_tuning& t) {
+    FILE* f = std::fopen(tuning_cache_path().c_str(), "a");
+    if (!f) return;
+    std::fprintf(f, "%s %d %u %u %u %u %.4f\n", key.c_str(), t.persistent, t.blocks_per_sm, t.block, t.stack,
+                 t.chunk_paths, t.ms);
+    std::fclose(f);
+}
+
+void apply_tuning(turner_ctx* ctx, const turner_tuning& t) {
+    ctx->traverse.persistent = t.persistent != 0;
+    ctx->traverse.blocks_per_sm = t.blocks_per_sm;
+    ctx->traverse.block = t.block == 256 ? 256 : 128;
+    ctx->traverse.stack = t.stack == 64 ? 64 : kStackCap;
+    ctx->chunk_paths = std::max<uint32_t>(1024, t.chunk_paths);
+}
+
+} // namespace
+
+extern "C" {
+
+int turner_set_tuning(turner_ctx* ctx, const turner_tuning* t) {
+    if (!ctx || !t) return TURNER_ERR_INVALID_ARG;
+    if ((t->block != 128 && t->block != 256) || (t->stack != 64 && t->stack != kStackCap) || t->blocks_per_sm > 64 ||
+        t->chunk_paths < 1024)
+        return TURNER_ERR_INVALID_ARG;
+    apply_tuning(ctx, *t);
+    return TURNER_OK;
+}
+
+int turner_get_tuning(turner_ctx* ctx, turner_tuning* t) {
+    if (!ctx || !t) return TURNER_ERR_INVALID_ARG;
+    t->persistent = ctx->traverse.persistent ? 1 : 0;
+    t->blocks_per_sm = ctx->traverse.blocks_per_sm;
+    t->block = ctx->traverse.block;
+    t->stack = ctx->traverse.stack;
+    t->chunk_paths = ctx->chunk_paths;
+    t->ms = 0;
+    t->candidates = 0;
+    return TURNER_OK;
+}
+
+int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, int force, turner_tuning* out) {
+    if (!ctx || !jobs || n_jobs == 0 || n_jobs > TURNER_MAX_JOBS) return TURNER_ERR_INVALID_ARG;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        const int st = check_job(ctx, jobs[j]);
+        if (st != TURNER_OK) return st;
+    }
+    TURNER_CK(cudaSetDevice(ctx->device));
+    const std::string key = tuning_key(ctx, jobs, n_jobs);
+    turner_tuning best{};
+    if (!force && tuning_lookup(key, best)) {
+        apply_tuning(ctx, best);
+        best.candidates = 0;
+        if (out) *out = best;
+        return TURNER_OK;
+    }
+    uint32_t max_height = 0;
+    uint64_t total_paths = 0, total_pixels = 0;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        max_height = std::max(max_height, ctx->scenes[jobs[j].scene_id]->view.height);
+        total_pixels += uint64_t(jobs[j].width) * jobs[j].height;
+        total_paths += uint64_t(jobs[j].width) * jobs[j].height * jobs[j].pixel_samples;
+    }
+    TURNER_CK(ctx->tune_out.ensure(sizeof(float4) * total_pixels));
+    std::vector<float*> outs(n_jobs);
+    uint64_t off = 0;
+    for (uint32_t j = 0; j < n_jobs; ++j) {
+        outs[j] = reinterpret_cast<float*>(ctx->tune_out.as<float4>() + off);
+        off += uint64_t(jobs[j].width) * jobs[j].height;
+    }
+    std::vector<turner_stats> st(n_jobs);
+    uint32_t tried = 0;
+    auto measure = [&](const turner_tuning& t, double& ms) -> int {
+        apply_tuning(ctx, t);
+        double best_ms = 1e300;
+        for (int rep = 0; rep < 2; ++rep) {   // the first run warms caches and allocates the workspace
+            const int s = turner_render(ctx, jobs, n_jobs, outs.data(), st.data(), TURNER_DEVICE_BUFFERS);
+            if (s != TURNER_OK) return s;
+            if (rep) best_ms = st[0].device_ms;
+        }
+        ms = best_ms;
+        ++tried;
+        return TURNER_OK;
+    };
+    // coordinate descent from the defaults, one knob at a time
+    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 0};
+    int s = measure(cur, cur.ms);
+    if (s != TURNER_OK) return s;
+    const uint32_t blocks[] = {128, 256};
+    const uint32_t per_sm[] = {0, 8, 6, 4};
+    const uint32_t stacks[] = {kStackCap, 64};
+    const uint32_t chunks[] = {1u << 24, 1u << 22, 1u << 20};
+    auto try_value = [&](auto setter, const auto& values) -> int {
+        for (const auto v : values) {
+            turner_tuning cand = cur;
+            if (!setter(cand, v)) continue;
+            double ms = 0;
+            const int r = measure(cand, ms);
+            if (r != TURNER_OK) return r;
+            if (ms < cur.ms * 0.99) {
+                cur = cand;
+                cur.ms = ms;
+            }
+        }
+        return TURNER_OK;
+    };
+    s = try_value([&](turner_tuning& t, uint32_t v) { if (t.block == v) return false; t.block = v; return true; }, blocks);
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) { if (t.blocks_per_sm == v) return false; t.blocks_per_sm = v; return true; },
+                      per_sm);
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.stack == v || v < max_height) return false;
+                t.stack = v;
+                return true;
+            }, stacks);
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.chunk_paths == v || (v > total_paths && t.chunk_paths >= total_paths)) return false;
+                t.chunk_paths = v;
+                return true;
+            }, chunks);
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, int v) { if (t.persistent == v) return false; t.persistent = v; return true; },
+                      std::vector<int>{0});
+    if (s != TURNER_OK) return s;
+    cur.candidates = tried;
+    apply_tuning(ctx, cur);
+    tuning_store(key, cur);
+    if (out) *out = cur;
     return TURNER_OK;
 }
 

@@ -61,6 +61,8 @@ struct Chunk {
 struct TraverseCfg {
     bool persistent = true;
     unsigned blocks_per_sm = 0;   // 0: as many as are resident
+    unsigned block = 128;         // threads per block of the persistent kernels: 128 or 256
+    unsigned stack = kStackCap;   // traversal stack entries: 64 or kStackCap (128)
     uint32_t* work = nullptr;
 };
 

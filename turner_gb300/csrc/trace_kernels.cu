@@ -302,12 +302,12 @@ struct SoaSrc {             // turner_intersect batches
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
 // while rays of very different lengths are traversed. MULTI: every ray names
 // its job and is traced in that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI>
-__global__ void __launch_bounds__(kBlock) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK>
+__global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
                                                      uint32_t* __restrict__ work) {
     const uint32_t n = src.count();
-    uint32_t st_node[kStackCap];
-    float st_enter[kStackCap], st_exit[kStackCap];
+    uint32_t st_node[STACK];
+    float st_enter[STACK], st_exit[STACK];
     TravState s;
     uint32_t cur = 0;
     bool active = false, exhausted = false;
@@ -399,13 +399,13 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(const JobDesc* __restrict
 inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
 // Resident blocks per SM x SMs for a persistent kernel (cached per kernel).
-template <class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap) {
+template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap) {
     static int sms = 0, per_sm = 0;
     if (sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, 0);
         sms = std::max(1, sms);
         per_sm = std::max(1, per_sm);
     }
@@ -413,12 +413,29 @@ template <class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap
     return static_cast<unsigned>(sms) * per;
 }
 
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK>
+void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
+                        const TraverseCfg& cfg, cudaStream_t stream) {
+    auto kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK>;
+    const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
+    const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm), std::max(1u, need));
+    kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work);
+}
+
+// Dispatch on the tuned block size and stack depth. The stack must hold the
+// scene's traversal depth (checked on upload against the largest, 128); the
+// batch planner only selects 64 when every scene fits.
 template <class Src, bool ANY, bool FAST, bool MULTI>
 void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
                   const TraverseCfg& cfg, cudaStream_t stream) {
-    auto kernel = k_traverse<Src, ANY, FAST, MULTI>;
-    const unsigned grid = std::min(persistent_grid(kernel, cfg.blocks_per_sm), std::max(1u, grid_for(capacity)));
-    kernel<<<grid, kBlock, 0, stream>>>(single, jobs, src, cfg.work);
+    const bool small_stack = cfg.stack == 64;
+    if (cfg.block == 256) {
+        if (small_stack) run_traverse_shape<Src, ANY, FAST, MULTI, 256, 64>(single, jobs, src, capacity, cfg, stream);
+        else run_traverse_shape<Src, ANY, FAST, MULTI, 256, kStackCap>(single, jobs, src, capacity, cfg, stream);
+    } else {
+        if (small_stack) run_traverse_shape<Src, ANY, FAST, MULTI, 128, 64>(single, jobs, src, capacity, cfg, stream);
+        else run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap>(single, jobs, src, capacity, cfg, stream);
+    }
 }
 
 // One thread per queue slot (the non-persistent launch shape).
