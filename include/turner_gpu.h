@@ -274,6 +274,32 @@ uint64_t turner_graph_launch_count(turner_ctx* ctx);
 int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t passes, double* out_rgba_mean,
                              uint64_t* total_samples, uint32_t flags);
 
+/* ------------------------------------------------- learned proposal */
+/* A small MLP predicting, per hit point, an 8-lobe von Mises-Fisher mixture
+ * over bounce directions (no counterpart in the reference, whose bounces are
+ * uniform on the hemisphere). BF16 weights on tcgen05 tensor cores with FP32
+ * accumulation; trained with Adam on (features, direction, weight) samples.
+ *   features  9 floats per sample: position in [0,1]^3 (scene box), shading
+ *             normal, albedo
+ *   output    40 floats per sample: 8 x (direction, log concentration, logit)
+ *   loss      mean over samples of -weight * log q(direction)
+ * Parameters: TURNER_GUIDE_PARAMS floats, W1 b1 ... W5 b5 (W row-major
+ * [out x in]; layers 80->64->64->64->64->40). */
+#define TURNER_GUIDE_PARAMS 20264
+typedef struct turner_guide turner_guide;
+int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out);
+void turner_guide_destroy(turner_guide* guide);
+/* set != 0: load params (host, TURNER_GUIDE_PARAMS floats); 0: read them. */
+int turner_guide_params(turner_guide* guide, float* params, int set);
+/* Host buffers: features n*9 in, out n*40 out. */
+int turner_guide_forward(turner_guide* guide, const float* features, uint32_t n, float* out);
+/* Sum over samples of d(-w log q)/d params into grad (host), and the summed loss. */
+int turner_guide_gradient(turner_guide* guide, const float* features, const float* dirs, const float* weights,
+                          uint32_t n, float* grad, float* loss);
+/* `steps` Adam steps (learning rate lr) on one batch; *loss = mean loss of the last. */
+int turner_guide_train(turner_guide* guide, const float* features, const float* dirs, const float* weights,
+                       uint32_t n, float lr, uint32_t steps, float* loss);
+
 /* ---------------------------------------------------------- host tree */
 /* SAH kd-tree of [WH06] Algorithm 4 with the reference's constants and
  * tie-breaking (lib/kdtree.cpp:124-467): the node words and triangle records

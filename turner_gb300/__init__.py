@@ -126,6 +126,12 @@ def _lib() -> C.CDLL:
         "turner_render": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.POINTER(_P), C.POINTER(Stats), C.c_uint32]),
         "turner_render_accumulate": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, _P, C.POINTER(C.c_uint64),
                                                C.c_uint32]),
+        "turner_guide_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
+        "turner_guide_destroy": (None, [_P]),
+        "turner_guide_params": (C.c_int, [_P, _P, C.c_int]),
+        "turner_guide_forward": (C.c_int, [_P, _P, C.c_uint32, _P]),
+        "turner_guide_gradient": (C.c_int, [_P, _P, _P, _P, C.c_uint32, _P, C.POINTER(C.c_float)]),
+        "turner_guide_train": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(C.c_float)]),
         "turner_kdtree_build": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, C.POINTER(_P)]),
         "turner_kdtree_num_nodes": (C.c_uint32, [_P]),
         "turner_kdtree_num_triangles": (C.c_uint32, [_P]),
@@ -381,6 +387,65 @@ class Context:
         ptrs = (_P * len(jobs))(*outs)
         _check(_lib().turner_render(self._h, arr, len(jobs), ptrs, stats, flags), "turner_render")
         return images, list(stats)
+
+
+GUIDE_PARAMS = 20264
+
+
+class Guide:
+    """The learned bounce proposal (BF16 MLP on tcgen05, vMF-mixture head)."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self._ctx = ctx   # keeps the context alive
+        self._h = _P()
+        _check(_lib().turner_guide_create(ctx._h, seed, C.byref(self._h)), "turner_guide_create")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.turner_guide_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(GUIDE_PARAMS, np.float32)
+        _check(_lib().turner_guide_params(self._h, _ptr(p), 0), "turner_guide_params")
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        q = np.ascontiguousarray(p, np.float32)
+        assert q.size == GUIDE_PARAMS
+        _check(_lib().turner_guide_params(self._h, _ptr(q), 1), "turner_guide_params")
+
+    def forward(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, 9)
+        out = np.empty((f.shape[0], 40), np.float32)
+        _check(_lib().turner_guide_forward(self._h, _ptr(f), f.shape[0], _ptr(out)), "turner_guide_forward")
+        return out
+
+    def gradient(self, features, dirs, weights):
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, 9)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        g = np.empty(GUIDE_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(_lib().turner_guide_gradient(self._h, _ptr(f), _ptr(d), _ptr(w), f.shape[0], _ptr(g), C.byref(loss)),
+               "turner_guide_gradient")
+        return g, loss.value
+
+    def train(self, features, dirs, weights, lr: float = 1e-3, steps: int = 1) -> float:
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, 9)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        loss = C.c_float()
+        _check(_lib().turner_guide_train(self._h, _ptr(f), _ptr(d), _ptr(w), f.shape[0], lr, steps, C.byref(loss)),
+               "turner_guide_train")
+        return loss.value
 
 
 def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, pixel_samples: int = 1,

@@ -33,6 +33,7 @@ GXX_COMMON = ["-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-I", str(ROOT 
 CUDA_UNITS = [
     (CSRC / "trace_kernels.cu", ["-fmad=false"]),
     (CSRC / "capi.cu", []),
+    (CSRC / "guide.cu", []),
 ]
 HOST_UNITS = [
     CSRC / "host" / "scenes.cpp",

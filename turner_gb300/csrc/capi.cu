@@ -271,6 +271,15 @@ void turner_destroy(turner_ctx* ctx) {
 
 int turner_last_device_error(turner_ctx* ctx) { return ctx ? TURNER_OK : TURNER_ERR_INVALID_ARG; }
 
+} // extern "C"
+
+namespace turner {
+cudaStream_t ctx_stream(turner_ctx* ctx) { return ctx->stream; }
+int ctx_device(turner_ctx* ctx) { return ctx->device; }
+} // namespace turner
+
+extern "C" {
+
 uint64_t turner_launch_count(turner_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 const char* turner_last_error_message(turner_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }

@@ -1,0 +1,660 @@
+// Learned bounce proposal: the MLP's forward, backward and Adam kernels.
+//
+// Forward (k_mlp_forward): persistent CTAs of 128 threads take tiles of 128
+// samples, one sample per thread. The encoded inputs and every hidden
+// activation stay in shared memory as BF16 in the core-matrix K-major layout
+// (tc.cuh); thread 0 issues tcgen05.mma (M = 128, N = 64 or 48, K in steps of
+// 16) into a TMEM accumulator, commits to an mbarrier, and each warp reads
+// its 32 lanes back with tcgen05.ld to add the bias, apply ReLU and write the
+// next layer's operand.
+//
+// Backward (k_mlp_backward): per tile, the vMF-mixture head gradient of the
+// loss -c log q(w) (one thread per sample), then per layer from the top:
+// dW += dY^T X and db += sum dY on the CUDA cores from shared memory (FP32),
+// and dX = dY W on the tensor cores (a second BF16 copy of the weights,
+// transposed), masked by ReLU'. Each CTA accumulates its gradient in shared
+// memory and adds it to the global one once.
+//
+// Every mbarrier wait is bounded; a timeout sets *err and the kernel drains
+// its outstanding MMA (bounded), frees its TMEM and returns.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "guide.cuh"
+#include "kernels.h"
+#include "tc.cuh"
+#include "turner_gpu.h"
+
+namespace turner {
+namespace guide {
+
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = 64;
+
+struct Weights {
+    const uint8_t* fwd;      // packed BF16 forward operands (kFwdBytes)
+    const uint8_t* bwd;      // packed BF16 transposed operands (kBwdBytes)
+    const float* params;     // FP32 master (biases are read from here)
+};
+
+__device__ __forceinline__ void store_bf16(uint8_t* base, uint32_t off, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
+}
+
+// Issues the K / 16 MMAs of one layer and commits them to `mbar` (thread 0).
+__device__ __forceinline__ void issue_layer(uint32_t tmem, const uint8_t* a, const uint8_t* b, int K, int N,
+                                            uint64_t* mbar) {
+    const uint32_t sa = tc::smem_u32(a), sb = tc::smem_u32(b);
+    const uint32_t sbo = static_cast<uint32_t>(K / 8) * 128u;
+    const uint32_t idesc = tc::idesc_bf16(128, static_cast<uint32_t>(N));
+    for (int i = 0; i < K / 16; ++i) {
+        const uint64_t ad = tc::smem_desc(sa + 256u * i, 128u, sbo);
+        const uint64_t bd = tc::smem_desc(sb + 256u * i, 128u, sbo);
+        tc::mma_bf16(tmem, ad, bd, idesc, i > 0);
+    }
+    tc::mma_commit(mbar);
+}
+
+// ---------------------------------------------------------------- forward
+struct FwdSmem {
+    uint8_t w[kFwdBytes];
+    uint8_t act0[kIn * 128 * 2];       // 128 x 80 (also 128 x 64)
+    uint8_t act1[kHidden * 128 * 2];   // 128 x 64
+    float bias[4 * kHidden + kOut];
+    uint64_t mbar;
+    uint32_t tmem;
+    int abort;
+};
+
+// features: n x 9 floats (position in [0,1]^3, shading normal, albedo).
+// out: n x 40 FP32 head values (may be null). acts (training): n x 336 BF16,
+// the layer inputs X_0 (80) .. X_4 (64 each) per sample.
+__global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(uint32_t n, const float* __restrict__ features,
+                                                             Weights wts, float* __restrict__ out,
+                                                             __nv_bfloat16* __restrict__ acts, int* err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    FwdSmem& sm = *reinterpret_cast<FwdSmem*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights and biases to shared memory
+    for (int i = tid; i < kFwdBytes / 16; i += kThreads) {
+        reinterpret_cast<uint4*>(sm.w)[i] = reinterpret_cast<const uint4*>(wts.fwd)[i];
+    }
+    for (int l = 0, o = 0; l < kLayers; ++l) {
+        for (int i = tid; i < layer_out(l); i += kThreads) sm.bias[o + i] = wts.params[layer_b(l) + i];
+        o += layer_out(l);
+    }
+    if (tid == 0) {
+        sm.abort = 0;
+        tc::mbar_init(&sm.mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) tc::tmem_alloc(&sm.tmem, kTmemCols);
+    tc::fence_async_smem();
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tmem = sm.tmem;
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    uint32_t phase = 0;
+    const uint32_t tiles = (n + 127) / 128;
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
+        const uint32_t s = tile * 128 + tid;
+        const bool valid = s < n;
+        // encoded inputs, BF16, K-major 128 x 80
+        {
+            float f[kIn];
+            if (valid) {
+                const float* q = features + 9 * size_t(s);
+                const float p[3] = {q[0], q[1], q[2]}, nn[3] = {q[3], q[4], q[5]}, a[3] = {q[6], q[7], q[8]};
+                encode(p, nn, a, f);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kIn; ++k) f[k] = 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < kIn; ++k) {
+                store_bf16(sm.act0, tc::kmajor_offset(tid, k, kIn), f[k]);
+                if (acts && valid) acts[size_t(s) * 336 + k] = __float2bfloat16_rn(f[k]);
+            }
+        }
+        tc::fence_async_smem();
+        tc::tc_fence_before_sync();
+        __syncthreads();
+        tc::tc_fence_after_sync();
+
+        uint8_t* in = sm.act0;
+        uint8_t* outb = sm.act1;
+        int bias_o = 0;
+        for (int l = 0; l < kLayers; ++l) {
+            const int K = layer_in(l), N = layer_out_pad(l);
+            if (tid == 0) issue_layer(tmem, in, sm.w + fwd_off(l), K, N, &sm.mbar);
+            if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
+            phase ^= 1;
+            tc::tc_fence_after_sync();
+            __syncthreads();
+            if (sm.abort) break;
+            // epilogue: this thread's row, 16 columns at a time
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = c0 + j;
+                    if (l < kLayers - 1) {
+                        const float y = fmaxf(v[j] + sm.bias[bias_o + c], 0.f);
+                        store_bf16(outb, tc::kmajor_offset(tid, c, kHidden), y);
+                        if (acts && valid) acts[size_t(s) * 336 + 80 + 64 * l + c] = __float2bfloat16_rn(y);
+                    } else if (c < kOut && out && valid) {
+                        out[size_t(s) * kOut + c] = v[j] + sm.bias[bias_o + c];
+                    }
+                }
+            }
+            bias_o += layer_out(l);
+            tc::fence_async_smem();
+            tc::tc_fence_before_sync();
+            __syncthreads();
+            tc::tc_fence_after_sync();
+            uint8_t* t = in;
+            in = outb;
+            outb = t;
+        }
+    }
+    if (sm.abort && tid == 0) {
+        // drain: an MMA may still be in flight; wait once more (bounded)
+        tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---------------------------------------------------------------- backward
+struct BwdSmem {
+    uint8_t wt[kBwdBytes];             // W_l^T operands, layers 1..4 (0-based)
+    uint8_t dy_km[kHidden * 128 * 2];  // dY, BF16, K-major 128 x 64 (or 48)
+    float dy[128][kHidden + 1];        // dY, FP32, row per sample (+1 avoids bank conflicts)
+    __nv_bfloat16 x[128][kIn + 2];     // X_l, row per sample
+    float grad[kParams];               // this CTA's gradient
+    uint64_t mbar;
+    uint32_t tmem;
+    int abort;
+    float loss;
+};
+
+// Head gradient of L = -c log q(w): writes dL/d raw (40) and returns L.
+__device__ __forceinline__ float head_grad(const float raw[kOut], const float dir[3], float c, float g[kOut]) {
+    Mixture m;
+    decode(raw, m);
+    float p[kLobes], q = 0.f;
+#pragma unroll
+    for (int l = 0; l < kLobes; ++l) {
+        p[l] = vmf_pdf(m.mu[l], m.kappa[l], dir);
+        q += m.w[l] * p[l];
+    }
+    q = fmaxf(q, 1e-20f);
+    const float loss = -c * logf(q);
+    const float gq = -c / q;
+    float gw[kLobes], wg = 0.f;
+#pragma unroll
+    for (int l = 0; l < kLobes; ++l) {
+        gw[l] = gq * p[l];
+        wg += m.w[l] * gw[l];
+    }
+#pragma unroll
+    for (int l = 0; l < kLobes; ++l) {
+        const float a = gq * m.w[l] * p[l];   // dL/d log p_l
+        const float cosw = m.mu[l][0] * dir[0] + m.mu[l][1] * dir[1] + m.mu[l][2] * dir[2];
+        // d log p / d mu = kappa * w ; project onto the tangent of the unit sphere, / |raw|
+        float gm[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gm[k] = a * m.kappa[l] * dir[k];
+        const float dot = gm[0] * m.mu[l][0] + gm[1] * m.mu[l][1] + gm[2] * m.mu[l][2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) g[5 * l + k] = (gm[k] - dot * m.mu[l][k]) * m.inv_len[l];
+        const float k2 = m.kappa[l];
+        const float dlogp = 1.f / k2 - 2.f / expm1f(2.f * k2) + (cosw - 1.f);
+        g[5 * l + 3] = a * dlogp * m.kexp[l];
+        g[5 * l + 4] = m.w[l] * (gw[l] - wg);
+    }
+    return loss;
+}
+
+// features/acts/out as produced by k_mlp_forward for the same samples;
+// dirs: n x 3 unit directions; weight: n target weights c. grad += dLoss/dparams.
+__global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const __nv_bfloat16* __restrict__ acts,
+                                                              const float* __restrict__ out,
+                                                              const float* __restrict__ dirs,
+                                                              const float* __restrict__ weight, Weights wts,
+                                                              float* __restrict__ grad, float* __restrict__ loss_sum,
+                                                              int* err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kBwdBytes / 16; i += kThreads) {
+        reinterpret_cast<uint4*>(sm.wt)[i] = reinterpret_cast<const uint4*>(wts.bwd)[i];
+    }
+    for (int i = tid; i < kParams; i += kThreads) sm.grad[i] = 0.f;
+    if (tid == 0) {
+        sm.abort = 0;
+        sm.loss = 0.f;
+        tc::mbar_init(&sm.mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) tc::tmem_alloc(&sm.tmem, kTmemCols);
+    tc::fence_async_smem();
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tmem = sm.tmem;
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    uint32_t phase = 0;
+    const uint32_t tiles = (n + 127) / 128;
+    float my_loss = 0.f;
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
+        const uint32_t s = tile * 128 + tid;
+        const bool valid = s < n;
+        // head: dY of the output layer, 40 columns padded to 48
+        {
+            float g[kOut];
+            if (valid) {
+                float raw[kOut];
+#pragma unroll
+                for (int k = 0; k < kOut; ++k) raw[k] = out[size_t(s) * kOut + k];
+                const float d[3] = {dirs[3 * size_t(s)], dirs[3 * size_t(s) + 1], dirs[3 * size_t(s) + 2]};
+                my_loss += head_grad(raw, d, weight[s], g);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kOut; ++k) g[k] = 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < kOutPad; ++k) {
+                const float v = k < kOut ? g[k] : 0.f;
+                sm.dy[tid][k] = v;
+                store_bf16(sm.dy_km, tc::kmajor_offset(tid, k, kOutPad), v);
+            }
+        }
+        for (int l = kLayers - 1; l >= 0; --l) {
+            const int K_in = layer_in(l), n_out = layer_out(l), n_pad = layer_out_pad(l);
+            // X_l rows of this tile
+            for (int k = 0; k < K_in; ++k) {
+                sm.x[tid][k] = valid ? acts[size_t(s) * 336 + (l == 0 ? 0 : 80 + 64 * (l - 1)) + k]
+                                     : __float2bfloat16_rn(0.f);
+            }
+            tc::fence_async_smem();
+            tc::tc_fence_before_sync();
+            __syncthreads();
+            tc::tc_fence_after_sync();
+            // dX = dY W on the tensor cores (not needed below the first layer)
+            if (l > 0 && tid == 0) issue_layer(tmem, sm.dy_km, sm.wt + bwd_off(l), n_pad, K_in, &sm.mbar);
+            // dW_l += dY^T X_l, db_l += sum dY on the CUDA cores meanwhile
+            const int wbase = layer_w(l), bbase = layer_b(l);
+            for (int e = tid; e < n_out * K_in; e += kThreads) {
+                const int o = e / K_in, k = e - o * K_in;
+                float acc = 0.f;
+                for (int r = 0; r < 128; ++r) acc += sm.dy[r][o] * __bfloat162float(sm.x[r][k]);
+                sm.grad[wbase + e] += acc;
+            }
+            if (tid < n_out) {
+                float acc = 0.f;
+                for (int r = 0; r < 128; ++r) acc += sm.dy[r][tid];
+                sm.grad[bbase + tid] += acc;
+            }
+            if (l > 0) {
+                if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
+                phase ^= 1;
+                tc::tc_fence_after_sync();
+            }
+            __syncthreads();   // dY and X_l are no longer read
+            if (sm.abort || l == 0) break;
+            // dY of the layer below: dX masked by ReLU' (X_l > 0)
+            for (int c0 = 0; c0 < K_in; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = c0 + j;
+                    const float d = __bfloat162float(sm.x[tid][c]) > 0.f ? v[j] : 0.f;
+                    sm.dy[tid][c] = d;
+                    store_bf16(sm.dy_km, tc::kmajor_offset(tid, c, kHidden), d);
+                }
+            }
+            tc::fence_async_smem();
+            tc::tc_fence_before_sync();
+            __syncthreads();
+            tc::tc_fence_after_sync();
+        }
+    }
+    // loss and gradient out
+    for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_xor_sync(0xFFFFFFFFu, my_loss, off);
+    if ((tid & 31) == 0) atomicAdd(&sm.loss, my_loss);
+    if (sm.abort && tid == 0) tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+    for (int i = tid; i < kParams; i += kThreads) {
+        if (sm.grad[i] != 0.f) atomicAdd(grad + i, sm.grad[i]);
+    }
+    if (tid == 0 && loss_sum) atomicAdd(loss_sum, sm.loss);
+}
+
+// ------------------------------------------------------------ Adam + pack
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float scale,
+                       float bc1, float bc2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * scale;
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// BF16 operand tiles from the FP32 parameters.
+__global__ void k_pack(const float* __restrict__ p, uint8_t* __restrict__ fwd, uint8_t* __restrict__ bwd) {
+    const int l = blockIdx.y;
+    const int K = layer_in(l), out = layer_out(l), pad = layer_out_pad(l);
+    const float* W = p + layer_w(l);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < pad * K; e += gridDim.x * blockDim.x) {
+        const int r = e / K, k = e - r * K;   // forward: row = output, column = input
+        const float w = r < out ? W[r * K + k] : 0.f;
+        store_bf16(fwd + fwd_off(l), tc::kmajor_offset(r, k, K), w);
+        if (l > 0) {                          // backward: row = input k, column = output r
+            store_bf16(bwd + bwd_off(l), tc::kmajor_offset(k, r, pad), w);
+        }
+    }
+}
+
+size_t fwd_smem() { return sizeof(FwdSmem) + 1024; }
+size_t bwd_smem() { return sizeof(BwdSmem) + 1024; }
+
+} // namespace guide
+} // namespace turner
+
+// ===================================================================== C ABI
+using namespace turner;
+using namespace turner::guide;
+
+struct turner_guide {
+    turner_ctx* ctx = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    float* params = nullptr;   // FP32 master
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    uint8_t* fwd = nullptr;
+    uint8_t* bwd = nullptr;
+    float* loss = nullptr;
+    int* err = nullptr;
+    uint64_t step = 0;
+    // training-batch scratch, grown on demand
+    size_t cap = 0;
+    float* feat = nullptr;
+    float* dirs = nullptr;
+    float* wts = nullptr;
+    float* out = nullptr;
+    __nv_bfloat16* acts = nullptr;
+    int sms = 1;
+    double train_ms = 0, infer_ms = 0;
+    uint64_t train_steps = 0;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+    return e == cudaSuccess ? TURNER_OK : (e == cudaErrorMemoryAllocation ? TURNER_ERR_OUT_OF_MEMORY : TURNER_ERR_CUDA);
+}
+
+#define GCK(call)                                      \
+    do {                                               \
+        const cudaError_t e_ = (call);                 \
+        if (e_ != cudaSuccess) return cuda_status(e_); \
+    } while (0)
+
+int ensure_batch(turner_guide* g, size_t n) {
+    if (n <= g->cap) return TURNER_OK;
+    cudaFree(g->feat);
+    cudaFree(g->dirs);
+    cudaFree(g->wts);
+    cudaFree(g->out);
+    cudaFree(g->acts);
+    g->feat = g->dirs = g->wts = g->out = nullptr;
+    g->acts = nullptr;
+    g->cap = 0;
+    GCK(cudaMalloc(&g->feat, n * 9 * sizeof(float)));
+    GCK(cudaMalloc(&g->dirs, n * 3 * sizeof(float)));
+    GCK(cudaMalloc(&g->wts, n * sizeof(float)));
+    GCK(cudaMalloc(&g->out, n * kOut * sizeof(float)));
+    GCK(cudaMalloc(&g->acts, n * 336 * sizeof(__nv_bfloat16)));
+    g->cap = n;
+    return TURNER_OK;
+}
+
+int check_err(turner_guide* g) {
+    int e = 0;
+    GCK(cudaMemcpyAsync(&e, g->err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    GCK(cudaStreamSynchronize(g->stream));
+    if (e) {
+        cudaMemsetAsync(g->err, 0, sizeof(int), g->stream);
+        return TURNER_ERR_TIMEOUT;
+    }
+    return TURNER_OK;
+}
+
+unsigned grid_tiles(turner_guide* g, uint32_t n) {
+    return std::max(1u, std::min<unsigned>(static_cast<unsigned>(g->sms), (n + 127) / 128));
+}
+
+} // namespace
+
+namespace turner {
+namespace guide {
+
+// Device-buffer forward for the renderer (features n x 9 -> out n x 40).
+int forward_device(turner_guide* g, const float* feat, uint32_t n, float* out, cudaStream_t stream) {
+    if (n == 0) return TURNER_OK;
+    Weights w{g->fwd, g->bwd, g->params};
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, feat, w, out, nullptr, g->err);
+    return cuda_status(cudaGetLastError());
+}
+
+// One Adam step on n device-resident samples (features n x 9, dirs n x 3,
+// weights n); optional loss (mean of -c log q) copied out.
+int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n, float lr,
+                 cudaStream_t stream, float* loss_out) {
+    if (n == 0) return TURNER_OK;
+    int st = ensure_batch(g, n);
+    if (st != TURNER_OK) return st;
+    Weights w{g->fwd, g->bwd, g->params};
+    GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), stream));
+    GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), stream));
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, feat, w, g->out, g->acts, g->err);
+    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), stream>>>(n, g->acts, g->out, dirs, wts, w, g->grad,
+                                                                      g->loss, g->err);
+    g->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float bc1 = 1.f - std::pow(b1, static_cast<float>(g->step));
+    const float bc2 = 1.f - std::pow(b2, static_cast<float>(g->step));
+    k_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->params, g->grad, g->m, g->v, kParams, lr, b1, b2, 1e-8f,
+                                                      1.f / static_cast<float>(n), bc1, bc2);
+    k_pack<<<dim3(16, kLayers), 256, 0, stream>>>(g->params, g->fwd, g->bwd);
+    GCK(cudaGetLastError());
+    g->train_steps += 1;
+    if (loss_out) {
+        float l = 0;
+        GCK(cudaMemcpyAsync(&l, g->loss, sizeof(float), cudaMemcpyDeviceToHost, stream));
+        GCK(cudaStreamSynchronize(stream));
+        *loss_out = l / static_cast<float>(n);
+    }
+    return TURNER_OK;
+}
+
+} // namespace guide
+} // namespace turner
+
+namespace turner {
+cudaStream_t ctx_stream(turner_ctx* ctx);
+int ctx_device(turner_ctx* ctx);
+} // namespace turner
+
+extern "C" {
+
+int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
+    if (!ctx || !out) return TURNER_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto* g = new (std::nothrow) turner_guide;
+    if (!g) return TURNER_ERR_OUT_OF_MEMORY;
+    g->ctx = ctx;
+    g->device = turner::ctx_device(ctx);
+    g->stream = turner::ctx_stream(ctx);
+    cudaSetDevice(g->device);
+    cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device);
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&g->params, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g->m, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g->v, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g->grad, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g->fwd, kFwdBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&g->bwd, kBwdBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&g->loss, sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&g->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(fwd_smem()));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(bwd_smem()));
+    if (e != cudaSuccess) {
+        turner_guide_destroy(g);
+        return cuda_status(e);
+    }
+    // He-uniform initialisation (seeded splitmix64 stream), zero biases;
+    // lobe directions start spread by the random last layer.
+    std::vector<float> p(kParams, 0.f);
+    uint64_t s = seed ? seed : 1;
+    auto uni = [&s]() {
+        s += 0x9E3779B97F4A7C15ULL;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        return static_cast<float>(static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0));
+    };
+    for (int l = 0; l < kLayers; ++l) {
+        const int fan_in = l == 0 ? kInUsed : kHidden;
+        const float a = std::sqrt(6.f / static_cast<float>(fan_in));
+        for (int r = 0; r < layer_out(l); ++r) {
+            for (int k = 0; k < layer_in(l); ++k) {
+                const float w = (l == 0 && k >= kInUsed) ? 0.f : (2.f * uni() - 1.f) * a;
+                p[layer_w(l) + r * layer_in(l) + k] = w;
+            }
+        }
+    }
+    e = cudaMemcpy(g->params, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(g->m, 0, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(g->v, 0, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_pack<<<dim3(16, kLayers), 256, 0, g->stream>>>(g->params, g->fwd, g->bwd);
+        e = cudaStreamSynchronize(g->stream);
+    }
+    if (e != cudaSuccess) {
+        turner_guide_destroy(g);
+        return cuda_status(e);
+    }
+    *out = g;
+    return TURNER_OK;
+}
+
+void turner_guide_destroy(turner_guide* g) {
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (void* p : {static_cast<void*>(g->params), static_cast<void*>(g->m), static_cast<void*>(g->v),
+                    static_cast<void*>(g->grad), static_cast<void*>(g->fwd), static_cast<void*>(g->bwd),
+                    static_cast<void*>(g->loss), static_cast<void*>(g->err), static_cast<void*>(g->feat),
+                    static_cast<void*>(g->dirs), static_cast<void*>(g->wts), static_cast<void*>(g->out),
+                    static_cast<void*>(g->acts)}) {
+        if (p) cudaFree(p);
+    }
+    delete g;
+}
+
+int turner_guide_params(turner_guide* g, float* host, int set) {
+    if (!g || !host) return TURNER_ERR_INVALID_ARG;
+    cudaSetDevice(g->device);
+    if (set) {
+        GCK(cudaMemcpyAsync(g->params, host, kParams * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+        k_pack<<<dim3(16, kLayers), 256, 0, g->stream>>>(g->params, g->fwd, g->bwd);
+        GCK(cudaGetLastError());
+    } else {
+        GCK(cudaMemcpyAsync(host, g->params, kParams * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    }
+    GCK(cudaStreamSynchronize(g->stream));
+    return TURNER_OK;
+}
+
+int turner_guide_forward(turner_guide* g, const float* features, uint32_t n, float* out) {
+    if (!g || !features || !out) return TURNER_ERR_INVALID_ARG;
+    if (n == 0) return TURNER_OK;
+    cudaSetDevice(g->device);
+    int st = ensure_batch(g, n);
+    if (st != TURNER_OK) return st;
+    GCK(cudaMemcpyAsync(g->feat, features, n * 9 * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    st = guide::forward_device(g, g->feat, n, g->out, g->stream);
+    if (st != TURNER_OK) return st;
+    GCK(cudaMemcpyAsync(out, g->out, n * kOut * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    GCK(cudaStreamSynchronize(g->stream));
+    return check_err(g);
+}
+
+int turner_guide_gradient(turner_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
+                          float* grad_out, float* loss_out) {
+    if (!g || !features || !dirs || !weights || !grad_out || n == 0) return TURNER_ERR_INVALID_ARG;
+    cudaSetDevice(g->device);
+    int st = ensure_batch(g, n);
+    if (st != TURNER_OK) return st;
+    GCK(cudaMemcpyAsync(g->feat, features, n * 9 * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    GCK(cudaMemcpyAsync(g->dirs, dirs, n * 3 * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    GCK(cudaMemcpyAsync(g->wts, weights, n * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), g->stream));
+    GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), g->stream));
+    Weights w{g->fwd, g->bwd, g->params};
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), g->stream>>>(n, g->feat, w, g->out, g->acts, g->err);
+    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), g->stream>>>(n, g->acts, g->out, g->dirs, g->wts, w,
+                                                                         g->grad, g->loss, g->err);
+    GCK(cudaGetLastError());
+    GCK(cudaMemcpyAsync(grad_out, g->grad, kParams * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    float l = 0;
+    GCK(cudaMemcpyAsync(&l, g->loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    GCK(cudaStreamSynchronize(g->stream));
+    if (loss_out) *loss_out = l;
+    return check_err(g);
+}
+
+int turner_guide_train(turner_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
+                       float lr, uint32_t steps, float* loss_out) {
+    if (!g || !features || !dirs || !weights || n == 0) return TURNER_ERR_INVALID_ARG;
+    cudaSetDevice(g->device);
+    int st = ensure_batch(g, n);
+    if (st != TURNER_OK) return st;
+    GCK(cudaMemcpyAsync(g->feat, features, n * 9 * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    GCK(cudaMemcpyAsync(g->dirs, dirs, n * 3 * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    GCK(cudaMemcpyAsync(g->wts, weights, n * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    float loss = 0;
+    for (uint32_t i = 0; i < steps; ++i) {
+        st = guide::train_device(g, g->feat, g->dirs, g->wts, n, lr, g->stream, i + 1 == steps ? &loss : nullptr);
+        if (st != TURNER_OK) return st;
+    }
+    if (loss_out) *loss_out = loss;
+    return check_err(g);
+}
+
+} // extern "C"
