@@ -63,6 +63,10 @@ extern "C" {
  * (lib/sampling.h:20-32, weight 2*cos); COSINE is cosine-weighted. */
 #define TURNER_SAMPLING_UNIFORM 0
 #define TURNER_SAMPLING_COSINE 1
+/* GUIDED: the context's learned proposal (turner_set_guide), mixed 1/2 with
+ * cosine sampling so the pdf stays positive on the hemisphere; estimator
+ * f cos / p. No reference counterpart. */
+#define TURNER_SAMPLING_GUIDED 2
 
 /* ------------------------------------------------------------- records */
 
@@ -299,6 +303,17 @@ int turner_guide_gradient(turner_guide* guide, const float* features, const floa
 /* `steps` Adam steps (learning rate lr) on one batch; *loss = mean loss of the last. */
 int turner_guide_train(turner_guide* guide, const float* features, const float* dirs, const float* weights,
                        uint32_t n, float lr, uint32_t steps, float* loss);
+
+/* Binds a proposal to the context for jobs with TURNER_SAMPLING_GUIDED
+ * (guide may be NULL to unbind). train != 0: online training during
+ * turner_render / turner_render_accumulate: after every pass (chunk), the
+ * pass's recorded bounces (about records_per_pass of them, >= 128; 0 keeps
+ * the current value, default 2^18) get their target weight (incident
+ * radiance times f cos / p, from the rest of the path) and one Adam step with
+ * learning rate lr runs. Training renders are not captured into graphs. */
+int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, uint32_t records_per_pass);
+/* Adam steps taken during renders, the last mean loss, device time of training. */
+int turner_guide_stats(turner_ctx* ctx, uint64_t* steps, float* last_loss, double* train_ms);
 
 /* ---------------------------------------------------------- host tree */
 /* SAH kd-tree of [WH06] Algorithm 4 with the reference's constants and

@@ -39,6 +39,7 @@ TRAVERSAL_PARITY = 0
 TRAVERSAL_FAST = 1
 SAMPLING_UNIFORM = 0
 SAMPLING_COSINE = 1
+SAMPLING_GUIDED = 2
 
 SCENE_ROOM = 0
 SCENE_SPHERE_ROOM = 1
@@ -127,6 +128,8 @@ def _lib() -> C.CDLL:
         "turner_render_accumulate": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, _P, C.POINTER(C.c_uint64),
                                                C.c_uint32]),
         "turner_guide_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
+        "turner_set_guide": (C.c_int, [_P, _P, C.c_int, C.c_float, C.c_uint32]),
+        "turner_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
         "turner_guide_destroy": (None, [_P]),
         "turner_guide_params": (C.c_int, [_P, _P, C.c_int]),
         "turner_guide_forward": (C.c_int, [_P, _P, C.c_uint32, _P]),
@@ -359,6 +362,16 @@ class Context:
 
     def set_tuning(self, t: Tuning) -> None:
         _check(_lib().turner_set_tuning(self._h, C.byref(t)), "turner_set_tuning")
+
+    def set_guide(self, guide: "Guide | None", train: bool = False, lr: float = 1e-3, records: int = 0) -> None:
+        _check(_lib().turner_set_guide(self._h, guide._h if guide is not None else None, 1 if train else 0, lr,
+                                       records), "turner_set_guide")
+
+    def guide_stats(self) -> tuple[int, float, float]:
+        """(Adam steps during renders, last mean loss, training device ms)."""
+        steps, loss, ms = C.c_uint64(), C.c_float(), C.c_double()
+        _check(_lib().turner_guide_stats(self._h, C.byref(steps), C.byref(loss), C.byref(ms)), "turner_guide_stats")
+        return steps.value, loss.value, ms.value
 
     def set_graph_mode(self, always: bool) -> None:
         _check(_lib().turner_set_graph_mode(self._h, 1 if always else 0), "turner_set_graph_mode")

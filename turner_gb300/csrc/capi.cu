@@ -1,5 +1,6 @@
 // C ABI of the GB300 path-tracing core: contexts, scene upload with
 // validation, batched intersection and the wavefront render loop.
+#include "guide.cuh"
 #include "kernels.h"
 #include "turner_gpu.h"
 
@@ -64,9 +65,18 @@ struct turner_ctx {
     uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
     uint64_t acc_samples = 0, acc_passes = 0;
     bool use_graph = false;            // capture single-job renders too
+    // learned proposal used by jobs with TURNER_SAMPLING_GUIDED
+    turner_guide* guide = nullptr;
+    bool guide_train = false;
+    float guide_lr = 1e-3f;
+    uint32_t guide_records = 1u << 18;   // training samples per pass
+    DevBuf gfeat, gout, qa_rec, qb_rec, r_feat, r_dir, r_weight, r_path, r_lbefore, r_tafter, r_fcp, r_count;
+    uint64_t guide_steps = 0;
+    float guide_last_loss = 0.f;
+    double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
     TraverseCfg traverse;              // persistent traversal on by default
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_train0 = nullptr, ev_train1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
     uint64_t launches = 0;
     std::string last_error;
@@ -207,7 +217,10 @@ int check_job(turner_ctx* ctx, const turner_job& j) {
     if (!(j.camera.aspect > 0)) return TURNER_ERR_INVALID_ARG;
     if (j.monte_carlo_samples < 0 || j.n_lights < 0 || j.n_lights > 1) return TURNER_ERR_INVALID_ARG;
     if (j.monte_carlo_samples > 1) return TURNER_ERR_UNSUPPORTED;
-    if (j.sampling != TURNER_SAMPLING_UNIFORM && j.sampling != TURNER_SAMPLING_COSINE) return TURNER_ERR_INVALID_ARG;
+    if (j.sampling != TURNER_SAMPLING_UNIFORM && j.sampling != TURNER_SAMPLING_COSINE &&
+        j.sampling != TURNER_SAMPLING_GUIDED)
+        return TURNER_ERR_INVALID_ARG;
+    if (j.sampling == TURNER_SAMPLING_GUIDED && !ctx->guide) return TURNER_ERR_INVALID_ARG;
     if (j.traversal != TURNER_TRAVERSAL_PARITY && j.traversal != TURNER_TRAVERSAL_FAST) return TURNER_ERR_INVALID_ARG;
     if (uint64_t(j.width) * j.height > (1ull << 31)) return TURNER_ERR_TOO_LARGE;
     if (j.max_depth > 64) return TURNER_ERR_TOO_LARGE;
@@ -249,6 +262,8 @@ int turner_create(turner_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_train0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_train1);
     if (e != cudaSuccess) {
         delete ctx;
         return map_cuda(e);
@@ -265,6 +280,8 @@ void turner_destroy(turner_ctx* ctx) {
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_train0) cudaEventDestroy(ctx->ev_train0);
+    if (ctx->ev_train1) cudaEventDestroy(ctx->ev_train1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -450,6 +467,7 @@ struct Batch {
     bool single_scene = true;
     SceneView single{};
     uint32_t max_height = 0;         // deepest traversal stack any scene needs
+    bool guided = false;             // some job samples with the learned proposal
 };
 
 int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4* const* outs, bool tone_map,
@@ -470,6 +488,7 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
         b.levels = std::max(b.levels, d.max_depth + 1);
         if (jobs[j].scene_id != jobs[0].scene_id) b.single_scene = false;
         b.max_height = std::max(b.max_height, d.sc.height);
+        if (d.sampling == TURNER_SAMPLING_GUIDED) b.guided = true;
     }
     b.total_pixels = pixels;
     b.single = b.table[0].sc;
@@ -511,6 +530,23 @@ int ensure_workspace(turner_ctx* ctx, const Batch& b) {
     TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * 4 * size_t(b.levels + 1) * b.chunks.size()));
     TURNER_CK(ctx->jobtab.ensure(sizeof(JobDesc) * b.table.size()));
     TURNER_CK(ctx->jobcnt.ensure(sizeof(unsigned long long) * 2 * b.table.size()));
+    if (b.guided) {
+        TURNER_CK(ctx->gfeat.ensure(sizeof(float) * 9 * size_t(cap)));
+        TURNER_CK(ctx->gout.ensure(sizeof(float) * guide::kOut * size_t(cap)));
+        if (ctx->guide_train) {
+            const size_t rc = ctx->guide_records;
+            TURNER_CK(ctx->qa_rec.ensure(sizeof(uint32_t) * cap));
+            TURNER_CK(ctx->qb_rec.ensure(sizeof(uint32_t) * cap));
+            TURNER_CK(ctx->r_feat.ensure(sizeof(float) * 9 * rc));
+            TURNER_CK(ctx->r_dir.ensure(sizeof(float) * 3 * rc));
+            TURNER_CK(ctx->r_weight.ensure(sizeof(float) * rc));
+            TURNER_CK(ctx->r_path.ensure(sizeof(uint32_t) * rc));
+            TURNER_CK(ctx->r_lbefore.ensure(sizeof(float) * rc));
+            TURNER_CK(ctx->r_tafter.ensure(sizeof(float) * rc));
+            TURNER_CK(ctx->r_fcp.ensure(sizeof(float) * rc));
+            TURNER_CK(ctx->r_count.ensure(sizeof(uint32_t)));
+        }
+    }
     return TURNER_OK;
 }
 
@@ -528,10 +564,18 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
     const SceneView* single = b.single_scene ? &b.single : nullptr;
     int fast = 1;
     for (const JobDesc& d : b.table) fast &= d.traversal == TURNER_TRAVERSAL_FAST ? 1 : 0;
+    const bool train = b.guided && ctx->guide_train;
     const RayQueue qa{ctx->qa[0].as<float4>(), ctx->qa[1].as<float4>(), ctx->qa[2].as<float4>(),
-                      ctx->qa[3].as<uint2>(), nullptr};
+                      ctx->qa[3].as<uint2>(), nullptr, train ? ctx->qa_rec.as<uint32_t>() : nullptr};
     const RayQueue qb{ctx->qb[0].as<float4>(), ctx->qb[1].as<float4>(), ctx->qb[2].as<float4>(),
-                      ctx->qb[3].as<uint2>(), nullptr};
+                      ctx->qb[3].as<uint2>(), nullptr, train ? ctx->qb_rec.as<uint32_t>() : nullptr};
+    const GuideQueue gq{b.guided ? ctx->gfeat.as<float>() : nullptr, b.guided ? ctx->gout.as<float>() : nullptr};
+    Records recs{};
+    if (train) {
+        recs = Records{ctx->r_feat.as<float>(), ctx->r_dir.as<float>(), ctx->r_weight.as<float>(),
+                       ctx->r_path.as<uint32_t>(), ctx->r_lbefore.as<float>(), ctx->r_tafter.as<float>(),
+                       ctx->r_fcp.as<float>(), ctx->r_count.as<uint32_t>(), ctx->guide_records, 0};
+    }
     ShadowQueue sh{ctx->shq[0].as<float4>(), ctx->shq[1].as<float4>(), ctx->shq[2].as<float4>(),
                    ctx->shjob.as<uint32_t>(), nullptr};
     for (size_t ci = 0; ci < b.chunks.size(); ++ci) {
@@ -539,6 +583,12 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
         uint32_t* cnt = counters + stride * ci;   // [queued rays | shadow rays | trace work | shadow work]
         RayQueue cur = qa, nxt = qb;
         cur.count = cnt;
+        if (train) {
+            // keep about guide_records of this pass's bounces, spread over all paths
+            const double bounces = double(c.n_paths) * std::max(1, b.levels - 1);
+            recs.keep = static_cast<uint32_t>(std::min(16777216.0, 16777216.0 * ctx->guide_records / bounces));
+            TURNER_CK(cudaMemsetAsync(recs.count, 0, sizeof(uint32_t), ctx->stream));
+        }
         {
             KernelTimer kt(ctx, TURNER_KERNEL_CAMERA);
             launch_camera(jobs, n_jobs, c, cur, ctx->L.as<float4>(), ctx->stream);
@@ -555,10 +605,16 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                 KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
                 launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_paths, fast, trace_cfg, ctx->stream);
             }
+            if (b.guided && depth + 1 < b.levels) {
+                launch_guide_features(jobs, depth, cur, ctx->hits.as<Hit>(), gq.feat, c.n_paths, ctx->stream);
+                const int gs = guide::forward_queue(ctx->guide, gq.feat, cur.count, c.n_paths, gq.out, ctx->stream);
+                if (gs != TURNER_OK) return gs;
+                ctx->launches += 2;
+            }
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
-                launch_shade(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts,
-                             c.n_paths, ctx->stream);
+                launch_shade(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts, gq,
+                             recs, c.n_paths, ctx->stream);
             }
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
@@ -572,6 +628,29 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             else launch_resolve(jobs, n_jobs, c, ctx->L.as<float4>(), ctx->stream);
         }
         TURNER_CK(cudaGetLastError());
+        if (train) {
+            // online training: this pass's bounces, weighted by the radiance they brought back
+            int gs = guide::finalize_records(recs.count, recs.cap, ctx->L.as<float4>(), recs.path, recs.l_before,
+                                             recs.t_after, recs.fcos_pdf, recs.weight, ctx->stream);
+            if (gs != TURNER_OK) return gs;
+            uint32_t n_rec = 0;
+            TURNER_CK(cudaMemcpyAsync(&n_rec, recs.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+            TURNER_CK(cudaEventRecord(ctx->ev_train0, ctx->stream));
+            TURNER_CK(cudaStreamSynchronize(ctx->stream));
+            n_rec = std::min(n_rec, recs.cap);
+            if (n_rec >= 128) {
+                gs = guide::train_device(ctx->guide, recs.feat, recs.dir, recs.weight, n_rec, ctx->guide_lr,
+                                         ctx->stream, &ctx->guide_last_loss);
+                if (gs != TURNER_OK) return gs;
+                ctx->guide_steps += 1;
+                ctx->launches += 4;
+                TURNER_CK(cudaEventRecord(ctx->ev_train1, ctx->stream));
+                TURNER_CK(cudaEventSynchronize(ctx->ev_train1));
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ctx->ev_train0, ctx->ev_train1);
+                ctx->guide_train_ms += ms;
+            }
+        }
     }
     return TURNER_OK;
 }
@@ -659,7 +738,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
     int st = plan_batch(ctx, jobs, n_jobs, outs.data(), true, b);
     if (st != TURNER_OK) return st;
     for (uint32_t j = 0; j < n_jobs; ++j) b.table[j].tone_map = jobs[j].linear_output ? 0 : 1;
-    st = run_batch(ctx, b, nullptr, stats, n_jobs > 1 || ctx->use_graph);
+    st = run_batch(ctx, b, nullptr, stats, (n_jobs > 1 || ctx->use_graph) && !(b.guided && ctx->guide_train));
     if (st != TURNER_OK) return st;
     if (flags == TURNER_HOST_BUFFERS) {
         for (uint32_t j = 0; j < n_jobs; ++j) {
@@ -696,7 +775,7 @@ int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t pa
         Batch b;
         st = plan_batch(ctx, &jp, 1, nullptr, false, b);
         if (st != TURNER_OK) return st;
-        st = run_batch(ctx, b, ctx->acc.as<double4>(), nullptr, ctx->use_graph);
+        st = run_batch(ctx, b, ctx->acc.as<double4>(), nullptr, ctx->use_graph && !(b.guided && ctx->guide_train));
         if (st != TURNER_OK) return st;
         ctx->acc_passes += 1;
         ctx->acc_samples += job->pixel_samples;
@@ -902,6 +981,23 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
     apply_tuning(ctx, cur);
     tuning_store(key, cur);
     if (out) *out = cur;
+    return TURNER_OK;
+}
+
+int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, uint32_t records_per_pass) {
+    if (!ctx || (train && !guide) || !(lr >= 0.f) || (train && records_per_pass < 128)) return TURNER_ERR_INVALID_ARG;
+    ctx->guide = guide;
+    ctx->guide_train = train != 0 && guide;
+    ctx->guide_lr = lr;
+    if (records_per_pass) ctx->guide_records = records_per_pass;
+    return TURNER_OK;
+}
+
+int turner_guide_stats(turner_ctx* ctx, uint64_t* steps, float* last_loss, double* train_ms) {
+    if (!ctx) return TURNER_ERR_INVALID_ARG;
+    if (steps) *steps = ctx->guide_steps;
+    if (last_loss) *last_loss = ctx->guide_last_loss;
+    if (train_ms) *train_ms = ctx->guide_train_ms;
     return TURNER_OK;
 }
 

@@ -74,12 +74,16 @@ struct FwdSmem {
 // features: n x 9 floats (position in [0,1]^3, shading normal, albedo).
 // out: n x 40 FP32 head values (may be null). acts (training): n x 336 BF16,
 // the layer inputs X_0 (80) .. X_4 (64 each) per sample.
-__global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(uint32_t n, const float* __restrict__ features,
-                                                             Weights wts, float* __restrict__ out,
-                                                             __nv_bfloat16* __restrict__ acts, int* err) {
+// n_dev (optional): the sample count is read from device memory (a queue
+// length), capped at n.
+__global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(uint32_t n, const uint32_t* __restrict__ n_dev,
+                                                             const float* __restrict__ features, Weights wts,
+                                                             float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
+                                                             int* err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& sm = *reinterpret_cast<FwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    if (n_dev) n = min(n, *n_dev);
     // weights and biases to shared memory
     for (int i = tid; i < kFwdBytes / 16; i += kThreads) {
         reinterpret_cast<uint4*>(sm.w)[i] = reinterpret_cast<const uint4*>(wts.fwd)[i];
@@ -463,7 +467,42 @@ namespace guide {
 int forward_device(turner_guide* g, const float* feat, uint32_t n, float* out, cudaStream_t stream) {
     if (n == 0) return TURNER_OK;
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, feat, w, out, nullptr, g->err);
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, out, nullptr, g->err);
+    return cuda_status(cudaGetLastError());
+}
+
+// Forward over a ray queue whose length is on the device (at most cap).
+int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uint32_t cap, float* out,
+                  cudaStream_t stream) {
+    if (cap == 0) return TURNER_OK;
+    Weights w{g->fwd, g->bwd, g->params};
+    k_mlp_forward<<<grid_tiles(g, cap), kThreads, fwd_smem(), stream>>>(cap, n_dev, feat, w, out, nullptr, g->err);
+    return cuda_status(cudaGetLastError());
+}
+
+// Target weights of the recorded bounces: the incident radiance along the
+// sampled direction is what the rest of the path added after the bounce,
+// divided by the throughput after it: L_in = (L_end - L_before) / T_after;
+// weight = L_in * f cos / p (the integrand over the sampling pdf, luminance).
+__global__ void k_finalize_records(const uint32_t* __restrict__ count, uint32_t cap, const float4* __restrict__ L,
+                                   const uint32_t* __restrict__ path, const float* __restrict__ l_before,
+                                   const float* __restrict__ t_after, const float* __restrict__ fcos_pdf,
+                                   float* __restrict__ weight) {
+    const uint32_t n = min(*count, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 l = L[path[i]];
+        const float lum = 0.2126f * l.x + 0.7152f * l.y + 0.0722f * l.z;
+        const float t = t_after[i];
+        const float lin = t > 0.f ? fmaxf(lum - l_before[i], 0.f) / t : 0.f;
+        weight[i] = fminf(lin * fcos_pdf[i], 1e4f);
+    }
+}
+
+int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const uint32_t* path,
+                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight,
+                     cudaStream_t stream) {
+    k_finalize_records<<<(cap + 255) / 256, 256, 0, stream>>>(count, cap, L, path, l_before, t_after, fcos_pdf,
+                                                              weight);
     return cuda_status(cudaGetLastError());
 }
 
@@ -477,7 +516,7 @@ int train_device(turner_guide* g, const float* feat, const float* dirs, const fl
     Weights w{g->fwd, g->bwd, g->params};
     GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), stream));
     GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), stream));
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, feat, w, g->out, g->acts, g->err);
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, g->out, g->acts, g->err);
     k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), stream>>>(n, g->acts, g->out, dirs, wts, w, g->grad,
                                                                       g->loss, g->err);
     g->step += 1;
@@ -627,7 +666,7 @@ int turner_guide_gradient(turner_guide* g, const float* features, const float* d
     GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), g->stream));
     GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), g->stream));
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), g->stream>>>(n, g->feat, w, g->out, g->acts, g->err);
+    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), g->stream>>>(n, nullptr, g->feat, w, g->out, g->acts, g->err);
     k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), g->stream>>>(n, g->acts, g->out, g->dirs, g->wts, w,
                                                                          g->grad, g->loss, g->err);
     GCK(cudaGetLastError());

@@ -16,6 +16,30 @@ struct RayQueue {
     float4* T;        // path throughput (RGBA)
     uint2* rng;       // bounce stream state
     uint32_t* count;  // number of valid entries (device)
+    uint32_t* rec;    // training record of the bounce that spawned the ray, or kNoRecord (may be null)
+};
+
+constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
+constexpr int kSamplingGuided = 2;   // TURNER_SAMPLING_GUIDED
+
+// Learned-proposal data per ray-queue slot (guided jobs only).
+struct GuideQueue {
+    float* feat;      // 9 floats: position in [0,1]^3 (scene box), shading normal, albedo
+    float* out;       // 40 floats: mixture parameters from the network
+};
+
+// Training samples recorded at guided bounces during a pass.
+struct Records {
+    float* feat;      // 9 per record (network input)
+    float* dir;       // 3 per record (sampled direction)
+    float* weight;    // target weight, filled after the pass
+    uint32_t* path;   // chunk-local path index
+    float* l_before;  // luminance of the path's radiance before the bounce's continuation
+    float* t_after;   // luminance of the throughput after the bounce
+    float* fcos_pdf;  // luminance of f cos / p for the bounce
+    uint32_t* count;
+    uint32_t cap;
+    uint32_t keep;    // record a bounce when its stream's next 32 bits are below keep
 };
 
 // Shadow-ray queue: one entry per hit with the light in front of the surface.
@@ -76,10 +100,15 @@ void launch_camera(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const R
                    cudaStream_t stream);
 void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& q, Hit* hits, uint32_t capacity,
                   int fast, const TraverseCfg& cfg, cudaStream_t stream);
-// job_counts (optional): per job {traced rays, shadow rays}, 64-bit
+// job_counts (optional): per job {traced rays, shadow rays}, 64-bit.
+// gq / recs: learned-proposal inputs and training records (null pointers
+// when no job of the batch samples with the learned proposal).
 void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
-                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
-                  cudaStream_t stream);
+                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, const GuideQueue& gq,
+                  const Records& recs, uint32_t capacity, cudaStream_t stream);
+// Network inputs for the hits of guided jobs that will bounce (zeros elsewhere).
+void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, const Hit* hits, float* feat,
+                           uint32_t capacity, cudaStream_t stream);
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
                    const TraverseCfg& cfg, cudaStream_t stream);
 void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream);
@@ -87,4 +116,20 @@ void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const 
 void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, double4* acc,
                        cudaStream_t stream);
 
+} // namespace turner
+
+struct turner_guide;
+
+namespace turner {
+namespace guide {
+// Host entry points of guide.cu used by the render loop (all asynchronous on
+// `stream` except train_device's optional loss readback).
+int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uint32_t cap, float* out,
+                  cudaStream_t stream);
+int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const uint32_t* path,
+                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight,
+                     cudaStream_t stream);
+int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n, float lr,
+                 cudaStream_t stream, float* loss_out);
+} // namespace guide
 } // namespace turner

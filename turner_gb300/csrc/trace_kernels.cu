@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "device.cuh"
+#include "guide.cuh"
 #include "kernels.h"
 
 namespace turner {
@@ -110,7 +111,53 @@ __global__ void __launch_bounds__(kBlock) k_camera(const JobDesc* __restrict__ j
     q.d[i] = make_float4(d.x, d.y, d.z, __uint_as_float(j));
     q.T[i] = make_float4(1.f, 1.f, 1.f, 1.f);
     q.rng[i] = make_uint2(static_cast<uint32_t>(bs), static_cast<uint32_t>(bs >> 32));
+    if (q.rec) q.rec[i] = kNoRecord;
     L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ float luminance(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// Shading normal of a hit: Triangle::interpolate_normal(1 - s - t, s, t)
+// (lib/triangle.h:54-56). Shared by k_shade and the network inputs.
+__device__ __forceinline__ float3 shading_normal(const float4& s0, const float4& s1, const float4& s2, const Hit& h) {
+    const float w0 = 1.f - h.s - h.t;
+    const float nx = w0 * s0.x + h.s * s1.x + h.t * s2.x;
+    const float ny = w0 * s0.y + h.s * s1.y + h.t * s2.y;
+    const float nz = w0 * s0.z + h.s * s1.z + h.t * s2.z;
+    const float inv_len = 1 / sqrtf(nx * nx + ny * ny + nz * nz);
+    return make_float3(inv_len * nx, inv_len * ny, inv_len * nz);
+}
+
+__global__ void __launch_bounds__(kBlock) k_guide_features(const JobDesc* __restrict__ jobs, int depth, RayQueue q,
+                                                           const Hit* __restrict__ hits, float* __restrict__ feat) {
+    const uint32_t n = *q.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float f[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float4 d4 = q.d[i];
+        const JobDesc& job = jobs[__float_as_uint(d4.w)];
+        const Hit h = hits[i];
+        if (job.sampling == kSamplingGuided && depth < job.max_depth && job.mc > 0 && h.id < kMiss) {
+            const float4 o4 = q.o[i];
+            const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
+            const float4* rec = job.sc.shade + 4 * size_t(h.id);
+            const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2);
+            const float3 nrm = shading_normal(s0, s1, s2, h);
+            const float pp[3] = {p.x, p.y, p.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float ext = job.sc.hi[k] - job.sc.lo[k];
+                f[k] = ext > 0.f ? fminf(fmaxf((pp[k] - job.sc.lo[k]) / ext, 0.f), 1.f) : 0.5f;
+            }
+            f[3] = nrm.x;
+            f[4] = nrm.y;
+            f[5] = nrm.z;
+            f[6] = s0.w;
+            f[7] = s1.w;
+            f[8] = s2.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) feat[9 * size_t(i) + k] = f[k];
+    }
 }
 
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
@@ -119,7 +166,8 @@ __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(
 
 __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jobs, int depth, RayQueue in,
                                                   const Hit* __restrict__ hits, RayQueue out, ShadowQueue sh,
-                                                  float4* __restrict__ L, unsigned long long* __restrict__ job_counts) {
+                                                  float4* __restrict__ L, unsigned long long* __restrict__ job_counts,
+                                                  GuideQueue gq, Records recs) {
     const uint32_t n = *in.count;
     const uint32_t stride = gridDim.x * blockDim.x;
     // warp-uniform loop so every lane reaches the ballots
@@ -130,6 +178,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
         float4 sh_o, sh_d, sh_c, b_o, b_d, b_T;
         uint2 b_rng;
         uint32_t jidx = 0;
+        bool emit_record = false;
+        float rec_dir[3] = {0.f, 0.f, 0.f}, rec_t = 0.f, rec_fcp = 0.f;
+        uint32_t rec_path = 0;
         if (valid) {
             const Hit h = hits[i];
             const float4 o4 = in.o[i];
@@ -138,6 +189,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
             const JobDesc& job = jobs[jidx];
             const uint32_t path = __float_as_uint(o4.w);
             const float4 T = in.T[i];
+            if (in.rec) {
+                // the bounce that spawned this ray: radiance of the path before its continuation
+                const uint32_t r = in.rec[i];
+                if (r != kNoRecord) recs.l_before[r] = luminance(L[path]);
+            }
             if (h.id >= kMiss) {
                 // miss: trace() returns conf.bg_color (alpha 1)
                 L[path] = add4(L[path], mul4(T, make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f)));
@@ -146,13 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                 const float4* rec = job.sc.shade + 4 * size_t(h.id);
                 const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2), s3 = __ldg(rec + 3);
                 const float4 diffuse = make_float4(s0.w, s1.w, s2.w, s3.x);
-                // Triangle::interpolate_normal(1 - s - t, s, t) (lib/triangle.h:54-56)
-                const float w0 = 1.f - h.s - h.t;
-                const float nx = w0 * s0.x + h.s * s1.x + h.t * s2.x;
-                const float ny = w0 * s0.y + h.s * s1.y + h.t * s2.y;
-                const float nz = w0 * s0.z + h.s * s1.z + h.t * s2.z;
-                const float inv_len = 1 / sqrtf(nx * nx + ny * ny + nz * nz);
-                const float3 nrm = make_float3(inv_len * nx, inv_len * ny, inv_len * nz);
+                const float3 nrm = shading_normal(s0, s1, s2, h);
                 const float3 p2 = make_float3(p.x + 0.0001f * nrm.x, p.y + 0.0001f * nrm.y, p.z + 0.0001f * nrm.z);
                 const float4 Td = mul4(T, diffuse);
                 if (job.n_lights > 0) {
@@ -180,7 +230,52 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                     const float u1 = xorshift_float(rs);
                     const float u2 = xorshift_float(rs);
                     float x, y, z, weight;
-                    if (job.sampling == 0) {
+                    float3 dir;
+                    bool bounce = true;
+                    if (job.sampling == kSamplingGuided) {
+                        // learned proposal: 1/2 cosine about the normal, 1/2 the vMF mixture
+                        float raw[guide::kOut];
+#pragma unroll
+                        for (int k = 0; k < guide::kOut; ++k) raw[k] = gq.out[guide::kOut * size_t(i) + k];
+                        guide::Mixture mix;
+                        guide::decode(raw, mix);
+                        const float u_sel = xorshift_float(rs);
+                        const float ua = xorshift_float(rs);
+                        const float ub = xorshift_float(rs);
+                        const float uc = xorshift_float(rs);
+                        float w3[3];
+                        if (u_sel < 0.5f) {
+                            const float rr = sqrtf(ua);
+                            const float zz = sqrtf(fmaxf(0.f, 1.f - ua));
+                            const float phi = 6.28318548202514648438f * ub;
+                            const float xx = rr * cosf(phi), yy = rr * sinf(phi);
+                            w3[0] = m[0] * xx + m[1] * yy + m[2] * zz;
+                            w3[1] = m[3] * xx + m[4] * yy + m[5] * zz;
+                            w3[2] = m[6] * xx + m[7] * yy + m[8] * zz;
+                        } else {
+                            int l = 0;
+                            float acc = mix.w[0];
+                            while (l < guide::kLobes - 1 && uc > acc) acc += mix.w[++l];
+                            float rot[9];
+                            from_to_z(make_float3(mix.mu[l][0], mix.mu[l][1], mix.mu[l][2]), rot);
+                            guide::vmf_sample(mix.mu[l], mix.kappa[l], ua, ub, rot, w3);
+                        }
+                        const float cw = nrm.x * w3[0] + nrm.y * w3[1] + nrm.z * w3[2];
+                        const float pdf = 0.5f * guide::mixture_pdf(mix, w3) + 0.5f * fmaxf(cw, 0.f) * guide::kInvPi;
+                        bounce = cw > 0.f && pdf > 0.f;   // below the surface the integrand is 0
+                        weight = bounce ? cw * guide::kInvPi / pdf : 0.f;
+                        dir = make_float3(w3[0], w3[1], w3[2]);
+                        x = y = z = 0.f;
+                        if (bounce && recs.count) {
+                            const float u_keep = xorshift_float(rs);
+                            emit_record = u_keep * 16777216.f < static_cast<float>(recs.keep);
+                            rec_dir[0] = w3[0];
+                            rec_dir[1] = w3[1];
+                            rec_dir[2] = w3[2];
+                            rec_path = path;
+                            rec_fcp = luminance(diffuse) * weight;
+                        }
+                    } else if (job.sampling == 0) {
                         // sampling::hemisphere (lib/sampling.h:20-32)
                         z = u1;
                         const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
@@ -196,13 +291,16 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                         y = rr * sinf(phi);
                         weight = 1.f;
                     }
-                    const float3 dir = make_float3(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
-                                                   m[6] * x + m[7] * y + m[8] * z);
+                    if (job.sampling != kSamplingGuided) {
+                        dir = make_float3(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
+                                          m[6] * x + m[7] * y + m[8] * z);
+                    }
                     b_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
                     b_d = make_float4(dir.x, dir.y, dir.z, __uint_as_float(jidx));
                     b_T = scale4(weight, Td);
                     b_rng = make_uint2(static_cast<uint32_t>(rs), static_cast<uint32_t>(rs >> 32));
-                    emit_bounce = true;
+                    emit_bounce = bounce;
+                    rec_t = luminance(b_T);
                 }
             }
         }
@@ -223,12 +321,29 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
             sh.c[si] = sh_c;
             sh.job[si] = jidx;
         }
+        uint32_t b_rec = kNoRecord;
+        if (recs.count) {
+            const uint32_t ri = warp_append(recs.count, emit_record);
+            if (emit_record && ri < recs.cap) {
+                b_rec = ri;
+                const float* f = gq.feat + 9 * size_t(i);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) recs.feat[9 * size_t(ri) + k] = f[k];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) recs.dir[3 * size_t(ri) + k] = rec_dir[k];
+                recs.path[ri] = rec_path;
+                recs.t_after[ri] = rec_t;
+                recs.fcos_pdf[ri] = rec_fcp;
+                recs.l_before[ri] = 0.f;
+            }
+        }
         const uint32_t bi = warp_append(out.count, emit_bounce);
         if (emit_bounce) {
             out.o[bi] = b_o;
             out.d[bi] = b_d;
             out.T[bi] = b_T;
             out.rng[bi] = b_rng;
+            if (out.rec) out.rec[bi] = b_rec;
         }
     }
 }
@@ -505,9 +620,14 @@ void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& 
 }
 
 void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
-                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
-                  cudaStream_t stream) {
-    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts);
+                  const ShadowQueue& sh, float4* L, unsigned long long* job_counts, const GuideQueue& gq,
+                  const Records& recs, uint32_t capacity, cudaStream_t stream) {
+    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts, gq, recs);
+}
+
+void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, const Hit* hits, float* feat,
+                           uint32_t capacity, cudaStream_t stream) {
+    k_guide_features<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, q, hits, feat);
 }
 
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
