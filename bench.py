@@ -222,6 +222,68 @@ def run_batch64(args) -> None:
     ctx.close()
 
 
+def run_guide(args) -> None:
+    """Equal-time MSE of the learned proposal vs the plain cosine tracer.
+
+    Scene: the indirect-lit room (walls tessellated 64x64 per wall, a 1.5x1.5
+    baffle 0.3 below the point light, 40,998 triangles), side x side pixels,
+    max depth 5. Reference: FP64-accumulated cosine render with ref_spp samples.
+    Both tracers accumulate passes of pass_spp samples in FP64 until the same
+    wall-clock budget is spent; the learned tracer trains online inside that
+    budget (one Adam step on 2^18 recorded bounces per pass, lr 1e-3)."""
+    import turner_gb300 as tg
+
+    side, depth = args.guide_side, 5
+    ctx = tg.Context(0)
+    mesh = tg.make_scene(tg.SCENE_BAFFLE_ROOM, detail=64)
+    sid = ctx.upload_tree(tg.KDTree.from_mesh(mesh))
+
+    def job(sampling, spp, seed):
+        j = tg.make_job(sid, mesh, side, side, pixel_samples=spp, max_depth=depth, seed=seed, sampling=sampling)
+        j.linear_output = 1
+        return j
+
+    t0 = time.perf_counter()
+    ref, ref_spp = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 424242), max(1, args.ref_spp // 256))
+    ref_s = time.perf_counter() - t0
+
+    def mse(img):
+        return float(((img[..., :3] - ref[..., :3]) ** 2).mean())
+
+    def run(sampling, seed, guide=None):
+        if guide is not None:
+            ctx.set_guide(guide, train=False)
+        ctx.accumulate(job(sampling, args.pass_spp, seed), 1)   # warm-up pass (workspace), not trained on
+        if guide is not None:
+            ctx.set_guide(guide, train=True, lr=1e-3, records=1 << 18)
+        t = time.perf_counter()
+        img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
+        while time.perf_counter() - t < args.budget:
+            img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
+        return img, total, time.perf_counter() - t
+
+    plain, plain_spp, plain_s = run(tg.SAMPLING_COSINE, 7)
+    guide = tg.Guide(ctx, seed=11)
+    ctx.set_chunk_paths(max(1024, (side * side * args.pass_spp) // 4))   # 4 passes (training steps) per call
+    learned, learned_spp, learned_s = run(tg.SAMPLING_GUIDED, 7, guide)
+    steps, loss, train_ms = ctx.guide_stats()
+    ctx.set_guide(None)
+    m_plain, m_learned = mse(plain), mse(learned)
+    print(json.dumps({
+        "metric": "equal-time MSE vs FP64 reference, learned proposal vs cosine (indirect-lit room)",
+        "value": round(m_plain / m_learned, 4), "unit": "MSE ratio (plain / learned, higher is better)",
+        "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 MLP / f32 tracing", "data": "synthetic",
+        "config": {"workload": f"baffle room 40,998 triangles {side}x{side} depth {depth}",
+                   "reference_spp": int(ref_spp), "reference_s": round(ref_s, 2), "budget_s": args.budget,
+                   "pass_spp": args.pass_spp},
+        "plain": {"mse": m_plain, "spp": int(plain_spp), "wall_s": round(plain_s, 3)},
+        "learned": {"mse": m_learned, "spp": int(learned_spp), "wall_s": round(learned_s, 3),
+                    "adam_steps": int(steps), "last_loss": round(loss, 4), "train_ms": round(train_ms, 1)},
+    }))
+    guide.close()
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,13 +297,20 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="480x270 frame of the same scene (for profiler captures; not a bench line)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch64"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch64", "guide"])
+    ap.add_argument("--guide-side", type=int, default=512)
+    ap.add_argument("--ref-spp", type=int, default=8192)
+    ap.add_argument("--pass-spp", type=int, default=4)
+    ap.add_argument("--budget", type=float, default=3.0)
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
     if args.workload == "batch64":
         run_batch64(args)
+        return
+    if args.workload == "guide":
+        run_guide(args)
         return
     if args.small:
         global WIDTH, HEIGHT, WORKLOAD
