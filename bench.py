@@ -258,8 +258,13 @@ def run_guide(args) -> None:
             ctx.set_guide(guide, train=True, lr=1e-3, records=1 << 18)
         t = time.perf_counter()
         img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
+        training = guide is not None
         while time.perf_counter() - t < args.budget:
-            img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
+            if training and time.perf_counter() - t > args.train_fraction * args.budget:
+                ctx.set_guide(guide, train=False)   # the rest of the budget renders with the trained network
+                ctx.set_chunk_paths(1 << 24)
+                training = False
+            img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1 if training else 4)
         return img, total, time.perf_counter() - t
 
     plain, plain_spp, plain_s = run(tg.SAMPLING_COSINE, 7)
@@ -275,7 +280,7 @@ def run_guide(args) -> None:
         "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 MLP / f32 tracing", "data": "synthetic",
         "config": {"workload": f"baffle room 40,998 triangles {side}x{side} depth {depth}",
                    "reference_spp": int(ref_spp), "reference_s": round(ref_s, 2), "budget_s": args.budget,
-                   "pass_spp": args.pass_spp},
+                   "pass_spp": args.pass_spp, "train_fraction": args.train_fraction},
         "plain": {"mse": m_plain, "spp": int(plain_spp), "wall_s": round(plain_s, 3)},
         "learned": {"mse": m_learned, "spp": int(learned_spp), "wall_s": round(learned_s, 3),
                     "adam_steps": int(steps), "last_loss": round(loss, 4), "train_ms": round(train_ms, 1)},
@@ -302,6 +307,7 @@ def main() -> None:
     ap.add_argument("--ref-spp", type=int, default=8192)
     ap.add_argument("--pass-spp", type=int, default=4)
     ap.add_argument("--budget", type=float, default=3.0)
+    ap.add_argument("--train-fraction", type=float, default=0.3)
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")

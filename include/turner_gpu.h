@@ -246,13 +246,18 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
  *   blocks_per_sm  resident traversal blocks per SM (0 = occupancy limit)
  *   block          threads per traversal block (128 or 256)
  *   stack          traversal stack entries (64 or 128; 64 only if every scene fits)
- *   chunk_paths    paths in flight per render pass (queue length) */
+ *   chunk_paths    paths in flight per render pass (queue length)
+ *   mailbox        1: skip a triangle this ray tested in the last four tests
+ *                  (exact: a repeat cannot change the answer; 128-thread blocks)
+ *   min_blocks     12: cap traversal registers so 12 blocks fit per SM, 0: no cap */
 typedef struct turner_tuning {
     int32_t persistent;
     uint32_t blocks_per_sm;
     uint32_t block;
     uint32_t stack;
     uint32_t chunk_paths;
+    uint32_t mailbox;
+    uint32_t min_blocks;
     double ms;             /* device time of the batch with this configuration */
     uint32_t candidates;   /* configurations timed (0: taken from the cache)  */
 } turner_tuning;

@@ -139,14 +139,17 @@ def test_autotune_caches_and_keeps_images(ctx, scenes, tmp_path, monkeypatch):
     after, _ = ctx.render(jobs)
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
-    for shape in ({"block": 256, "stack": 64}, {"block": 128, "stack": 128}):
+    for shape in ({"block": 256, "stack": 64, "mailbox": 0, "min_blocks": 0},
+                  {"block": 128, "stack": 128, "mailbox": 1, "min_blocks": 12},
+                  {"block": 128, "stack": 64, "mailbox": 1, "min_blocks": 0}):
         tt = ctx.get_tuning()
-        tt.block, tt.stack = shape["block"], shape["stack"]
+        tt.block, tt.stack, tt.mailbox, tt.min_blocks = shape["block"], shape["stack"], shape["mailbox"], \
+            shape["min_blocks"]
         ctx.set_tuning(tt)
         again, _ = ctx.render(jobs)
         for a, b in zip(before, again):
             assert np.array_equal(a, b)
-    ctx.set_tuning(tg.Tuning(1, 0, 128, 128, 1 << 24, 0.0, 0))
+    ctx.set_tuning(tg.Tuning(1, 0, 128, 128, 1 << 24, 0, 0, 0.0, 0))
 
 
 def test_too_many_jobs_rejected(ctx, scenes):

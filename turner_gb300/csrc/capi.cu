@@ -841,8 +841,8 @@ bool tuning_lookup(const std::string& key, turner_tuning& t) {
     while (std::fgets(line, sizeof(line), f)) {
         char k[256];
         turner_tuning r{};
-        if (std::sscanf(line, "%255s %d %u %u %u %u %lf", k, &r.persistent, &r.blocks_per_sm, &r.block, &r.stack,
-                        &r.chunk_paths, &r.ms) == 7 && key == k) {
+        if (std::sscanf(line, "%255s %d %u %u %u %u %u %u %lf", k, &r.persistent, &r.blocks_per_sm, &r.block,
+                        &r.stack, &r.chunk_paths, &r.mailbox, &r.min_blocks, &r.ms) == 9 && key == k) {
             t = r;
             found = true;   // the last entry for a key wins
         }
@@ -854,8 +854,8 @@ bool tuning_lookup(const std::string& key, turner_tuning& t) {
 void tuning_store(const std::string& key, const turner_tuning& t) {
     FILE* f = std::fopen(tuning_cache_path().c_str(), "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %u %u %u %u %.4f\n", key.c_str(), t.persistent, t.blocks_per_sm, t.block, t.stack,
-                 t.chunk_paths, t.ms);
+    std::fprintf(f, "%s %d %u %u %u %u %u %u %.4f\n", key.c_str(), t.persistent, t.blocks_per_sm, t.block, t.stack,
+                 t.chunk_paths, t.mailbox, t.min_blocks, t.ms);
     std::fclose(f);
 }
 
@@ -864,6 +864,8 @@ void apply_tuning(turner_ctx* ctx, const turner_tuning& t) {
     ctx->traverse.blocks_per_sm = t.blocks_per_sm;
     ctx->traverse.block = t.block == 256 ? 256 : 128;
     ctx->traverse.stack = t.stack == 64 ? 64 : kStackCap;
+    ctx->traverse.mailbox = t.mailbox != 0;
+    ctx->traverse.min_blocks = t.min_blocks == 12 ? 12 : 0;
     ctx->chunk_paths = std::max<uint32_t>(1024, t.chunk_paths);
 }
 
@@ -874,7 +876,7 @@ extern "C" {
 int turner_set_tuning(turner_ctx* ctx, const turner_tuning* t) {
     if (!ctx || !t) return TURNER_ERR_INVALID_ARG;
     if ((t->block != 128 && t->block != 256) || (t->stack != 64 && t->stack != kStackCap) || t->blocks_per_sm > 64 ||
-        t->chunk_paths < 1024)
+        t->chunk_paths < 1024 || t->mailbox > 1 || (t->min_blocks != 0 && t->min_blocks != 12))
         return TURNER_ERR_INVALID_ARG;
     apply_tuning(ctx, *t);
     return TURNER_OK;
@@ -887,6 +889,8 @@ int turner_get_tuning(turner_ctx* ctx, turner_tuning* t) {
     t->block = ctx->traverse.block;
     t->stack = ctx->traverse.stack;
     t->chunk_paths = ctx->chunk_paths;
+    t->mailbox = ctx->traverse.mailbox ? 1 : 0;
+    t->min_blocks = ctx->traverse.min_blocks;
     t->ms = 0;
     t->candidates = 0;
     return TURNER_OK;
@@ -936,7 +940,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
         return TURNER_OK;
     };
     // coordinate descent from the defaults, one knob at a time
-    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 0};
+    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 0, 0, 0};
     int s = measure(cur, cur.ms);
     if (s != TURNER_OK) return s;
     const uint32_t blocks[] = {128, 256};
@@ -973,6 +977,18 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
                 t.chunk_paths = v;
                 return true;
             }, chunks);
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.mailbox == v || t.block != 128) return false;
+                t.mailbox = v;
+                return true;
+            }, std::vector<uint32_t>{1});
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.min_blocks == v || t.block != 128) return false;
+                t.min_blocks = v;
+                return true;
+            }, std::vector<uint32_t>{12});
     if (s == TURNER_OK)
         s = try_value([&](turner_tuning& t, int v) { if (t.persistent == v) return false; t.persistent = v; return true; },
                       std::vector<int>{0});

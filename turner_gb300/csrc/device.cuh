@@ -217,13 +217,34 @@ struct TravState {
     float tenter, texit;
     int sp;
     Hit best;
+    // the last four triangles tested by this ray. A triangle referenced by
+    // several leaves is tested again by the reference; the repeat gives the
+    // same r, which can no longer pass `r < best` (or newly satisfy r <= dist),
+    // so skipping it leaves the answer unchanged.
+    uint32_t mb[4];
+    uint32_t mb_next;
 };
+
+template <bool MAILBOX>
+__device__ __forceinline__ bool mailbox_seen(TravState& s, uint32_t id) {
+    if (!MAILBOX) return false;
+    if (id == s.mb[0] || id == s.mb[1] || id == s.mb[2] || id == s.mb[3]) return true;
+    const uint32_t k = s.mb_next & 3u;
+    s.mb[0] = k == 0 ? id : s.mb[0];
+    s.mb[1] = k == 1 ? id : s.mb[1];
+    s.mb[2] = k == 2 ? id : s.mb[2];
+    s.mb[3] = k == 3 ? id : s.mb[3];
+    s.mb_next = k + 1;
+    return false;
+}
 
 // fix_direction + root box test. false: the ray misses the scene box.
 __device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3 d, TravState& s) {
     s.nodes = sc.nodes;
     s.tri = sc.tri;
     s.best = Hit{kMiss, kFltMax, 0.f, 0.f};
+    s.mb[0] = s.mb[1] = s.mb[2] = s.mb[3] = kMiss;
+    s.mb_next = 0;
     const float3 fd = make_float3(d.x == 0.f ? kEps : d.x, d.y == 0.f ? kEps : d.y, d.z == 0.f ? kEps : d.z);
     s.o = o;
     s.d = d;
@@ -247,7 +268,7 @@ __device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3
 
 // One round: descend from s.node to a leaf, test its run, pop the next cell.
 // Returns true when the ray is finished (s.best holds the answer).
-template <bool ANY, bool FAST_EXIT>
+template <bool ANY, bool FAST_EXIT, bool MAILBOX = false>
 __device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* st_node, float* st_enter,
                                            float* st_exit) {
     const uint2* __restrict__ nodes = s.nodes;
@@ -280,13 +301,15 @@ __device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* s
     }
     for (;;) {
         float r, u, v;
-        if (triangle_test_bounded<ANY>(s.tri, w.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+        if (!mailbox_seen<MAILBOX>(s, w.y) &&
+            triangle_test_bounded<ANY>(s.tri, w.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
             s.best = Hit{w.y, r, u, v};
             if (ANY) return true;
         }
         if (w.x == 0xFFFFFFFFu) break;
         const uint32_t id2 = w.x >> 2;
-        if (triangle_test_bounded<ANY>(s.tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+        if (!mailbox_seen<MAILBOX>(s, id2) &&
+            triangle_test_bounded<ANY>(s.tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
             s.best = Hit{id2, r, u, v};
             if (ANY) return true;
         }

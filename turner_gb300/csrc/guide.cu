@@ -76,7 +76,7 @@ struct FwdSmem {
 // the layer inputs X_0 (80) .. X_4 (64 each) per sample.
 // n_dev (optional): the sample count is read from device memory (a queue
 // length), capped at n.
-__global__ void __launch_bounds__(kThreads, 1) k_mlp_forward(uint32_t n, const uint32_t* __restrict__ n_dev,
+__global__ void __launch_bounds__(kThreads, 2) k_mlp_forward(uint32_t n, const uint32_t* __restrict__ n_dev,
                                                              const float* __restrict__ features, Weights wts,
                                                              float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
                                                              int* err) {
@@ -454,8 +454,14 @@ int check_err(turner_guide* g) {
     return TURNER_OK;
 }
 
+// One CTA per SM for the backward pass (its shared memory fills an SM).
 unsigned grid_tiles(turner_guide* g, uint32_t n) {
     return std::max(1u, std::min<unsigned>(static_cast<unsigned>(g->sms), (n + 127) / 128));
+}
+
+// Two forward CTAs per SM: one's MMAs overlap the other's epilogue.
+unsigned grid_tiles_fwd(turner_guide* g, uint32_t n) {
+    return std::max(1u, std::min<unsigned>(2u * static_cast<unsigned>(g->sms), (n + 127) / 128));
 }
 
 } // namespace
@@ -467,7 +473,7 @@ namespace guide {
 int forward_device(turner_guide* g, const float* feat, uint32_t n, float* out, cudaStream_t stream) {
     if (n == 0) return TURNER_OK;
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, out, nullptr, g->err);
+    k_mlp_forward<<<grid_tiles_fwd(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, out, nullptr, g->err);
     return cuda_status(cudaGetLastError());
 }
 
@@ -476,7 +482,7 @@ int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uin
                   cudaStream_t stream) {
     if (cap == 0) return TURNER_OK;
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles(g, cap), kThreads, fwd_smem(), stream>>>(cap, n_dev, feat, w, out, nullptr, g->err);
+    k_mlp_forward<<<grid_tiles_fwd(g, cap), kThreads, fwd_smem(), stream>>>(cap, n_dev, feat, w, out, nullptr, g->err);
     return cuda_status(cudaGetLastError());
 }
 

@@ -87,6 +87,8 @@ struct TraverseCfg {
     unsigned blocks_per_sm = 0;   // 0: as many as are resident
     unsigned block = 128;         // threads per block of the persistent kernels: 128 or 256
     unsigned stack = kStackCap;   // traversal stack entries: 64 or kStackCap (128)
+    bool mailbox = false;         // skip repeated tests of a triangle (128-thread blocks)
+    unsigned min_blocks = 0;      // 12: cap registers so that 12 blocks fit per SM (128-thread blocks)
     uint32_t* work = nullptr;
 };
 

@@ -417,9 +417,9 @@ struct SoaSrc {             // turner_intersect batches
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
 // while rays of very different lengths are traversed. MULTI: every ray names
 // its job and is traced in that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK>
-__global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
-                                                     uint32_t* __restrict__ work) {
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
+                                                           uint32_t* __restrict__ work) {
     const uint32_t n = src.count();
     uint32_t st_node[STACK];
     float st_enter[STACK], st_exit[STACK];
@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobD
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
-        if (active && trav_round<ANY, FAST>(s, tmax, st_node, st_enter, st_exit)) {
+        if (active && trav_round<ANY, FAST, MAILBOX>(s, tmax, st_node, st_enter, st_exit)) {
             src.store(cur, s.best);
             active = false;
         }
@@ -528,10 +528,10 @@ template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks
     return static_cast<unsigned>(sms) * per;
 }
 
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK>
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
 void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
                         const TraverseCfg& cfg, cudaStream_t stream) {
-    auto kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK>;
+    auto kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB>;
     const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
     const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm), std::max(1u, need));
     kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work);
@@ -545,12 +545,26 @@ void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, 
                   const TraverseCfg& cfg, cudaStream_t stream) {
     const bool small_stack = cfg.stack == 64;
     if (cfg.block == 256) {
-        if (small_stack) run_traverse_shape<Src, ANY, FAST, MULTI, 256, 64>(single, jobs, src, capacity, cfg, stream);
-        else run_traverse_shape<Src, ANY, FAST, MULTI, 256, kStackCap>(single, jobs, src, capacity, cfg, stream);
-    } else {
-        if (small_stack) run_traverse_shape<Src, ANY, FAST, MULTI, 128, 64>(single, jobs, src, capacity, cfg, stream);
-        else run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap>(single, jobs, src, capacity, cfg, stream);
+        if (small_stack) {
+            run_traverse_shape<Src, ANY, FAST, MULTI, 256, 64, false, 1>(single, jobs, src, capacity, cfg, stream);
+        } else {
+            run_traverse_shape<Src, ANY, FAST, MULTI, 256, kStackCap, false, 1>(single, jobs, src, capacity, cfg,
+                                                                                stream);
+        }
+        return;
     }
+    // 128-thread blocks: mailbox on/off x register cap for 12 resident blocks on/off
+#define TURNER_SHAPE(ST, MB, MINB) \
+    run_traverse_shape<Src, ANY, FAST, MULTI, 128, ST, MB, MINB>(single, jobs, src, capacity, cfg, stream)
+    const bool mb = cfg.mailbox, occ = cfg.min_blocks == 12;
+    if (small_stack) {
+        if (mb) { if (occ) TURNER_SHAPE(64, true, 12); else TURNER_SHAPE(64, true, 1); }
+        else { if (occ) TURNER_SHAPE(64, false, 12); else TURNER_SHAPE(64, false, 1); }
+    } else {
+        if (mb) { if (occ) TURNER_SHAPE(kStackCap, true, 12); else TURNER_SHAPE(kStackCap, true, 1); }
+        else { if (occ) TURNER_SHAPE(kStackCap, false, 12); else TURNER_SHAPE(kStackCap, false, 1); }
+    }
+#undef TURNER_SHAPE
 }
 
 // One thread per queue slot (the non-persistent launch shape).
