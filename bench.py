@@ -227,10 +227,14 @@ def run_guide(args) -> None:
 
     Scene: the indirect-lit room (walls tessellated 64x64 per wall, a 1.5x1.5
     baffle 0.3 below the point light, 40,998 triangles), side x side pixels,
-    max depth 5. Reference: FP64-accumulated cosine render with ref_spp samples.
+    max depth 5. Reference: FP64-accumulated cosine render with ref_spp samples,
+    in two independent halves whose difference estimates the reference's own
+    variance (reported, and removed in value_reference_noise_removed).
     Both tracers accumulate passes of pass_spp samples in FP64 until the same
     wall-clock budget is spent; the learned tracer trains online inside that
-    budget (one Adam step on 2^18 recorded bounces per pass, lr 1e-3)."""
+    budget (--guide-steps Adam steps per pass over about --guide-records of
+    the pass's bounces, lr --guide-lr) and its training passes count toward
+    its image."""
     import turner_gb300 as tg
 
     side, depth = args.guide_side, 5
@@ -243,9 +247,15 @@ def run_guide(args) -> None:
         j.linear_output = 1
         return j
 
+    # reference: two independent halves; their difference estimates the
+    # reference's own variance, which inflates both MSEs by the same amount
     t0 = time.perf_counter()
-    ref, ref_spp = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 424242), max(1, args.ref_spp // 256))
+    half = max(1, args.ref_spp // 512)
+    ref_a, spp_a = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 424242), half)
+    ref_b, spp_b = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 525252), half)
     ref_s = time.perf_counter() - t0
+    ref, ref_spp = 0.5 * (ref_a + ref_b), spp_a + spp_b
+    ref_var = float(((ref_a[..., :3] - ref_b[..., :3]) ** 2).mean() / 4)
 
     def mse(img):
         return float(((img[..., :3] - ref[..., :3]) ** 2).mean())
@@ -255,21 +265,20 @@ def run_guide(args) -> None:
             ctx.set_guide(guide, train=False)
         ctx.accumulate(job(sampling, args.pass_spp, seed), 1)   # warm-up pass (workspace), not trained on
         if guide is not None:
-            ctx.set_guide(guide, train=True, lr=1e-3, records=1 << 18)
+            ctx.set_guide(guide, train=True, lr=args.guide_lr, records=args.guide_records,
+                          steps_per_pass=args.guide_steps)
         t = time.perf_counter()
         img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
         training = guide is not None
         while time.perf_counter() - t < args.budget:
             if training and time.perf_counter() - t > args.train_fraction * args.budget:
                 ctx.set_guide(guide, train=False)   # the rest of the budget renders with the trained network
-                ctx.set_chunk_paths(1 << 24)
                 training = False
             img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1 if training else 4)
         return img, total, time.perf_counter() - t
 
     plain, plain_spp, plain_s = run(tg.SAMPLING_COSINE, 7)
     guide = tg.Guide(ctx, seed=11)
-    ctx.set_chunk_paths(max(1024, (side * side * args.pass_spp) // 4))   # 4 passes (training steps) per call
     learned, learned_spp, learned_s = run(tg.SAMPLING_GUIDED, 7, guide)
     steps, loss, train_ms = ctx.guide_stats()
     ctx.set_guide(None)
@@ -277,10 +286,14 @@ def run_guide(args) -> None:
     print(json.dumps({
         "metric": "equal-time MSE vs FP64 reference, learned proposal vs cosine (indirect-lit room)",
         "value": round(m_plain / m_learned, 4), "unit": "MSE ratio (plain / learned, higher is better)",
+        "value_reference_noise_removed": round((m_plain - ref_var) / (m_learned - ref_var), 4),
+        "reference_variance": ref_var,
         "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 MLP / f32 tracing", "data": "synthetic",
         "config": {"workload": f"baffle room 40,998 triangles {side}x{side} depth {depth}",
                    "reference_spp": int(ref_spp), "reference_s": round(ref_s, 2), "budget_s": args.budget,
-                   "pass_spp": args.pass_spp, "train_fraction": args.train_fraction},
+                   "pass_spp": args.pass_spp, "train_fraction": args.train_fraction,
+                   "records_per_pass": args.guide_records, "steps_per_pass": args.guide_steps,
+                   "lr": args.guide_lr},
         "plain": {"mse": m_plain, "spp": int(plain_spp), "wall_s": round(plain_s, 3)},
         "learned": {"mse": m_learned, "spp": int(learned_spp), "wall_s": round(learned_s, 3),
                     "adam_steps": int(steps), "last_loss": round(loss, 4), "train_ms": round(train_ms, 1)},
@@ -308,6 +321,9 @@ def main() -> None:
     ap.add_argument("--pass-spp", type=int, default=4)
     ap.add_argument("--budget", type=float, default=3.0)
     ap.add_argument("--train-fraction", type=float, default=0.3)
+    ap.add_argument("--guide-records", type=int, default=1 << 16)
+    ap.add_argument("--guide-lr", type=float, default=1e-3)
+    ap.add_argument("--guide-steps", type=int, default=4, help="Adam steps per training pass")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")

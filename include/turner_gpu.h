@@ -175,7 +175,10 @@ int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks
 #define TURNER_KERNEL_SHADOW 3    /* any-hit traversal of the shadow queue */
 #define TURNER_KERNEL_RESOLVE 4
 #define TURNER_KERNEL_INTERSECT 5
-#define TURNER_KERNEL_KINDS 6
+#define TURNER_KERNEL_GUIDE_FEATURES 6   /* network inputs of guided hits */
+#define TURNER_KERNEL_MLP_FORWARD 7      /* tcgen05 inference of the learned proposal */
+#define TURNER_KERNEL_GUIDE_TRAIN 8      /* record weights + one training step (timed always) */
+#define TURNER_KERNEL_KINDS 9
 int turner_set_profiling(turner_ctx* ctx, int on);
 /* Copies the accumulated milliseconds and launch counts per kind (arrays of
  * TURNER_KERNEL_KINDS; either may be NULL) and optionally resets them. */
@@ -315,9 +318,15 @@ int turner_guide_train(turner_guide* guide, const float* features, const float* 
  * pass's recorded bounces (about records_per_pass of them, >= 128; 0 keeps
  * the current value, default 2^18) get their target weight (incident
  * radiance times f cos / p, from the rest of the path) and one Adam step with
- * learning rate lr runs. Training renders are not captured into graphs. */
+ * learning rate lr runs, on the context's stream without a host
+ * synchronisation. Training renders are not captured into graphs. */
 int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, uint32_t records_per_pass);
-/* Adam steps taken during renders, the last mean loss, device time of training. */
+/* Adam steps per training pass (1..64, default 1), each over all of the
+ * pass's records: more steps per pass learn faster from the same samples. */
+int turner_set_guide_steps(turner_ctx* ctx, uint32_t steps_per_pass);
+/* Adam steps the bound proposal has taken (in renders and turner_guide_train),
+ * its last mean loss (both 0 when no proposal is bound; waits for the
+ * context's stream), and the device time of training during renders. */
 int turner_guide_stats(turner_ctx* ctx, uint64_t* steps, float* last_loss, double* train_ms);
 
 /* ---------------------------------------------------------- host tree */

@@ -35,7 +35,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("n", [1, 128, 293, 5000])
+@pytest.mark.parametrize("n", [1, 128, 293, 5000, 100_003])   # the last: several tiles per persistent CTA
 def test_forward_matches_oracle(ctx, n):
     g = tg.Guide(ctx, seed=3)
     p = mo.init_params(11).astype(np.float32)

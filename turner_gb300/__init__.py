@@ -49,7 +49,8 @@ SCENE_BAFFLE_SPHERE = 4
 
 TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
-KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect")
+KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect", "k_guide_features",
+                "k_mlp_forward", "guide_train")
 KERNEL_KINDS = len(KERNEL_NAMES)
 
 
@@ -130,6 +131,7 @@ def _lib() -> C.CDLL:
                                                C.c_uint32]),
         "turner_guide_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
         "turner_set_guide": (C.c_int, [_P, _P, C.c_int, C.c_float, C.c_uint32]),
+        "turner_set_guide_steps": (C.c_int, [_P, C.c_uint32]),
         "turner_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
         "turner_guide_destroy": (None, [_P]),
         "turner_guide_params": (C.c_int, [_P, _P, C.c_int]),
@@ -364,12 +366,14 @@ class Context:
     def set_tuning(self, t: Tuning) -> None:
         _check(_lib().turner_set_tuning(self._h, C.byref(t)), "turner_set_tuning")
 
-    def set_guide(self, guide: "Guide | None", train: bool = False, lr: float = 1e-3, records: int = 0) -> None:
+    def set_guide(self, guide: "Guide | None", train: bool = False, lr: float = 1e-3, records: int = 0,
+                  steps_per_pass: int = 1) -> None:
         _check(_lib().turner_set_guide(self._h, guide._h if guide is not None else None, 1 if train else 0, lr,
                                        records), "turner_set_guide")
+        _check(_lib().turner_set_guide_steps(self._h, steps_per_pass), "turner_set_guide_steps")
 
     def guide_stats(self) -> tuple[int, float, float]:
-        """(Adam steps during renders, last mean loss, training device ms)."""
+        """(Adam steps of the bound proposal, its last mean loss, training device ms in renders)."""
         steps, loss, ms = C.c_uint64(), C.c_float(), C.c_double()
         _check(_lib().turner_guide_stats(self._h, C.byref(steps), C.byref(loss), C.byref(ms)), "turner_guide_stats")
         return steps.value, loss.value, ms.value

@@ -70,13 +70,12 @@ struct turner_ctx {
     bool guide_train = false;
     float guide_lr = 1e-3f;
     uint32_t guide_records = 1u << 18;   // training samples per pass
+    uint32_t guide_steps_per_pass = 1;    // Adam steps on each pass's samples
     DevBuf gfeat, gout, qa_rec, qb_rec, r_feat, r_dir, r_weight, r_path, r_lbefore, r_tafter, r_fcp, r_count;
-    uint64_t guide_steps = 0;
-    float guide_last_loss = 0.f;
     double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
     TraverseCfg traverse;              // persistent traversal on by default
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_train0 = nullptr, ev_train1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
     uint64_t launches = 0;
     std::string last_error;
@@ -105,9 +104,9 @@ struct KernelTimer {
     int kind;
     size_t first = 0;
     bool on = false;
-    KernelTimer(turner_ctx* c, int k) : ctx(c), kind(k) {
+    KernelTimer(turner_ctx* c, int k, bool always = false) : ctx(c), kind(k) {
         ctx->launches += 1;
-        if (!ctx->profiling) return;
+        if (!ctx->profiling && !always) return;
         first = ctx->ev_used.size() * 2;
         while (ctx->ev_pool.size() < first + 2) {
             cudaEvent_t e;
@@ -131,6 +130,7 @@ void collect_kernel_times(turner_ctx* ctx) {
         if (cudaEventElapsedTime(&ms, ctx->ev_pool[u.second], ctx->ev_pool[u.second + 1]) == cudaSuccess) {
             ctx->kernel_ms[u.first] += ms;
             ctx->kernel_launches[u.first] += 1;
+            if (u.first == TURNER_KERNEL_GUIDE_TRAIN) ctx->guide_train_ms += ms;
         }
     }
     ctx->ev_used.clear();
@@ -262,8 +262,6 @@ int turner_create(turner_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_train0);
-    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_train1);
     if (e != cudaSuccess) {
         delete ctx;
         return map_cuda(e);
@@ -280,8 +278,6 @@ void turner_destroy(turner_ctx* ctx) {
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-    if (ctx->ev_train0) cudaEventDestroy(ctx->ev_train0);
-    if (ctx->ev_train1) cudaEventDestroy(ctx->ev_train1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -606,10 +602,16 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                 launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_paths, fast, trace_cfg, ctx->stream);
             }
             if (b.guided && depth + 1 < b.levels) {
-                launch_guide_features(jobs, depth, cur, ctx->hits.as<Hit>(), gq.feat, c.n_paths, ctx->stream);
-                const int gs = guide::forward_queue(ctx->guide, gq.feat, cur.count, c.n_paths, gq.out, ctx->stream);
+                {
+                    KernelTimer kt(ctx, TURNER_KERNEL_GUIDE_FEATURES);
+                    launch_guide_features(jobs, depth, cur, ctx->hits.as<Hit>(), gq.feat, c.n_paths, ctx->stream);
+                }
+                int gs;
+                {
+                    KernelTimer kt(ctx, TURNER_KERNEL_MLP_FORWARD);
+                    gs = guide::forward_queue(ctx->guide, gq.feat, cur.count, c.n_paths, gq.out, ctx->stream);
+                }
                 if (gs != TURNER_OK) return gs;
-                ctx->launches += 2;
             }
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
@@ -630,25 +632,17 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
         TURNER_CK(cudaGetLastError());
         if (train) {
             // online training: this pass's bounces, weighted by the radiance they brought back
+            // (no host synchronisation: the step reads the record count on the device and
+            // skips itself when fewer than 128 bounces were recorded)
+            KernelTimer kt(ctx, TURNER_KERNEL_GUIDE_TRAIN, true);
             int gs = guide::finalize_records(recs.count, recs.cap, ctx->L.as<float4>(), recs.path, recs.l_before,
                                              recs.t_after, recs.fcos_pdf, recs.weight, ctx->stream);
             if (gs != TURNER_OK) return gs;
-            uint32_t n_rec = 0;
-            TURNER_CK(cudaMemcpyAsync(&n_rec, recs.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-            TURNER_CK(cudaEventRecord(ctx->ev_train0, ctx->stream));
-            TURNER_CK(cudaStreamSynchronize(ctx->stream));
-            n_rec = std::min(n_rec, recs.cap);
-            if (n_rec >= 128) {
-                gs = guide::train_device(ctx->guide, recs.feat, recs.dir, recs.weight, n_rec, ctx->guide_lr,
-                                         ctx->stream, &ctx->guide_last_loss);
+            for (uint32_t k = 0; k < ctx->guide_steps_per_pass; ++k) {
+                gs = guide::train_device(ctx->guide, recs.feat, recs.dir, recs.weight, recs.cap, recs.count, 128,
+                                         ctx->guide_lr, ctx->stream, nullptr);
                 if (gs != TURNER_OK) return gs;
-                ctx->guide_steps += 1;
-                ctx->launches += 4;
-                TURNER_CK(cudaEventRecord(ctx->ev_train1, ctx->stream));
-                TURNER_CK(cudaEventSynchronize(ctx->ev_train1));
-                float ms = 0;
-                cudaEventElapsedTime(&ms, ctx->ev_train0, ctx->ev_train1);
-                ctx->guide_train_ms += ms;
+                ctx->launches += 5;   // prep, forward, backward, Adam, pack
             }
         }
     }
@@ -1009,10 +1003,21 @@ int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, 
     return TURNER_OK;
 }
 
+int turner_set_guide_steps(turner_ctx* ctx, uint32_t steps_per_pass) {
+    if (!ctx || steps_per_pass == 0 || steps_per_pass > 64) return TURNER_ERR_INVALID_ARG;
+    ctx->guide_steps_per_pass = steps_per_pass;
+    return TURNER_OK;
+}
+
 int turner_guide_stats(turner_ctx* ctx, uint64_t* steps, float* last_loss, double* train_ms) {
     if (!ctx) return TURNER_ERR_INVALID_ARG;
-    if (steps) *steps = ctx->guide_steps;
-    if (last_loss) *last_loss = ctx->guide_last_loss;
+    if (steps) *steps = 0;
+    if (last_loss) *last_loss = 0.f;
+    if (ctx->guide) {
+        TURNER_CK(cudaSetDevice(ctx->device));
+        const int st = guide::train_state(ctx->guide, steps, last_loss);
+        if (st != TURNER_OK) return st;
+    }
     if (train_ms) *train_ms = ctx->guide_train_ms;
     return TURNER_OK;
 }

@@ -1,12 +1,13 @@
 // Learned bounce proposal: the MLP's forward, backward and Adam kernels.
 //
-// Forward (k_mlp_forward): persistent CTAs of 128 threads take tiles of 128
-// samples, one sample per thread. The encoded inputs and every hidden
-// activation stay in shared memory as BF16 in the core-matrix K-major layout
-// (tc.cuh); thread 0 issues tcgen05.mma (M = 128, N = 64 or 48, K in steps of
-// 16) into a TMEM accumulator, commits to an mbarrier, and each warp reads
-// its 32 lanes back with tcgen05.ld to add the bias, apply ReLU and write the
-// next layer's operand.
+// Forward (k_mlp_forward): persistent CTAs of 256 threads (three per SM)
+// take tiles of 128 samples, two threads per sample. The encoded inputs and
+// every hidden activation stay in shared memory as BF16 in the core-matrix
+// K-major layout (tc.cuh), one buffer updated in place; thread 0 issues
+// tcgen05.mma (M = 128, N = 64 or 48, K in steps of 16) into a TMEM
+// accumulator, commits to an mbarrier, and each warp reads its 32 lanes and
+// half of the columns back with tcgen05.ld to add the bias, apply ReLU and
+// write the next layer's operand with 16-byte stores.
 //
 // Backward (k_mlp_backward): per tile, the vMF-mixture head gradient of the
 // loss -c log q(w) (one thread per sample), then per layer from the top:
@@ -61,35 +62,66 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, const uint8_t* a, con
 }
 
 // ---------------------------------------------------------------- forward
+constexpr int kFwdThreads = 256;   // two warps per TMEM lane quadrant
+constexpr int kFwdBlocksPerSm = 3;
+
 struct FwdSmem {
     uint8_t w[kFwdBytes];
-    uint8_t act0[kIn * 128 * 2];       // 128 x 80 (also 128 x 64)
-    uint8_t act1[kHidden * 128 * 2];   // 128 x 64
+    uint8_t act[kIn * 128 * 2];        // 128 x 80 inputs, then each layer's 128 x 64 output in place
     float bias[4 * kHidden + kOut];
     uint64_t mbar;
     uint32_t tmem;
     int abort;
 };
 
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Eight encoded inputs k = 8g .. 8g + 7 of one sample (see encode()): groups
+// 0-8 are four frequencies of one axis, group 9 the normal, albedo and padding.
+__device__ __forceinline__ uint4 encode_group(int g, const float p[3], const float nn[3], const float a[3]) {
+    float f[8];
+    if (g < 9) {
+        const int ax = g / 3, i0 = (g - ax * 3) * 4;
+        const float x = g < 3 ? p[0] : g < 6 ? p[1] : p[2];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sincospif(x * static_cast<float>(1 << (i0 + j)), &f[2 * j], &f[2 * j + 1]);
+    } else {
+        f[0] = nn[0]; f[1] = nn[1]; f[2] = nn[2];
+        f[3] = a[0]; f[4] = a[1]; f[5] = a[2];
+        f[6] = 0.f; f[7] = 0.f;
+    }
+    return make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
+                      pack_bf16x2(f[6], f[7]));
+}
+
 // features: n x 9 floats (position in [0,1]^3, shading normal, albedo).
 // out: n x 40 FP32 head values (may be null). acts (training): n x 336 BF16,
 // the layer inputs X_0 (80) .. X_4 (64 each) per sample.
 // n_dev (optional): the sample count is read from device memory (a queue
 // length), capped at n.
-__global__ void __launch_bounds__(kThreads, 2) k_mlp_forward(uint32_t n, const uint32_t* __restrict__ n_dev,
-                                                             const float* __restrict__ features, Weights wts,
-                                                             float* __restrict__ out, __nv_bfloat16* __restrict__ acts,
-                                                             int* err) {
+//
+// Thread t works on row t % 128 of the tile; the two threads of a row split
+// its input groups (5 each) and its output columns (32 each for hidden
+// layers; 32 and 16 of the padded 48 for the head), so every shared-memory
+// write is one 16-byte store of 8 BF16 values. A layer's output overwrites
+// its input in place: the MMAs have read it once their commit has arrived.
+__global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
+    uint32_t n, const uint32_t* __restrict__ n_dev, const float* __restrict__ features, Weights wts,
+    float* __restrict__ out, __nv_bfloat16* __restrict__ acts, int* err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& sm = *reinterpret_cast<FwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t row = static_cast<uint32_t>(tid & 127);
+    const int half = tid >> 7;
     if (n_dev) n = min(n, *n_dev);
-    // weights and biases to shared memory
-    for (int i = tid; i < kFwdBytes / 16; i += kThreads) {
+    for (int i = tid; i < kFwdBytes / 16; i += kFwdThreads) {
         reinterpret_cast<uint4*>(sm.w)[i] = reinterpret_cast<const uint4*>(wts.fwd)[i];
     }
     for (int l = 0, o = 0; l < kLayers; ++l) {
-        for (int i = tid; i < layer_out(l); i += kThreads) sm.bias[o + i] = wts.params[layer_b(l) + i];
+        for (int i = tid; i < layer_out(l); i += kFwdThreads) sm.bias[o + i] = wts.params[layer_b(l) + i];
         o += layer_out(l);
     }
     if (tid == 0) {
@@ -103,28 +135,30 @@ __global__ void __launch_bounds__(kThreads, 2) k_mlp_forward(uint32_t n, const u
     __syncthreads();
     tc::tc_fence_after_sync();
     const uint32_t tmem = sm.tmem;
-    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
     uint32_t phase = 0;
     const uint32_t tiles = (n + 127) / 128;
 
     for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
-        const uint32_t s = tile * 128 + tid;
+        const uint32_t s = tile * 128 + row;
         const bool valid = s < n;
-        // encoded inputs, BF16, K-major 128 x 80
+        uint4* const act_row = acts && valid ? reinterpret_cast<uint4*>(acts + size_t(s) * 336) : nullptr;
         {
-            float f[kIn];
+            float p[3] = {0.f, 0.f, 0.f}, nn[3] = {0.f, 0.f, 0.f}, a[3] = {0.f, 0.f, 0.f};
             if (valid) {
                 const float* q = features + 9 * size_t(s);
-                const float p[3] = {q[0], q[1], q[2]}, nn[3] = {q[3], q[4], q[5]}, a[3] = {q[6], q[7], q[8]};
-                encode(p, nn, a, f);
-            } else {
 #pragma unroll
-                for (int k = 0; k < kIn; ++k) f[k] = 0.f;
+                for (int k = 0; k < 3; ++k) {
+                    p[k] = q[k];
+                    nn[k] = q[3 + k];
+                    a[k] = q[6 + k];
+                }
             }
-#pragma unroll
-            for (int k = 0; k < kIn; ++k) {
-                store_bf16(sm.act0, tc::kmajor_offset(tid, k, kIn), f[k]);
-                if (acts && valid) acts[size_t(s) * 336 + k] = __float2bfloat16_rn(f[k]);
+#pragma unroll 1
+            for (int g = half * 5; g < half * 5 + 5; ++g) {
+                const uint4 v = valid ? encode_group(g, p, nn, a) : make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4*>(sm.act + tc::kmajor_offset(row, 8 * g, kIn)) = v;
+                if (act_row) act_row[g] = v;
             }
         }
         tc::fence_async_smem();
@@ -132,30 +166,55 @@ __global__ void __launch_bounds__(kThreads, 2) k_mlp_forward(uint32_t n, const u
         __syncthreads();
         tc::tc_fence_after_sync();
 
-        uint8_t* in = sm.act0;
-        uint8_t* outb = sm.act1;
         int bias_o = 0;
+#pragma unroll 1
         for (int l = 0; l < kLayers; ++l) {
             const int K = layer_in(l), N = layer_out_pad(l);
-            if (tid == 0) issue_layer(tmem, in, sm.w + fwd_off(l), K, N, &sm.mbar);
+            if (tid == 0) issue_layer(tmem, sm.act, sm.w + fwd_off(l), K, N, &sm.mbar);
             if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
             phase ^= 1;
             tc::tc_fence_after_sync();
             __syncthreads();
             if (sm.abort) break;
-            // epilogue: this thread's row, 16 columns at a time
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                float v[16];
-                tc::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), v);
+            const uint32_t c0 = static_cast<uint32_t>(half * 32);
+            if (l < kLayers - 1) {
+                float v[32];
+                tc::tmem_ld16(tmem + lane_base + c0, v);
+                tc::tmem_ld16(tmem + lane_base + c0 + 16u, v + 16);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int c = c0 + j;
-                    if (l < kLayers - 1) {
-                        const float y = fmaxf(v[j] + sm.bias[bias_o + c], 0.f);
-                        store_bf16(outb, tc::kmajor_offset(tid, c, kHidden), y);
-                        if (acts && valid) acts[size_t(s) * 336 + 80 + 64 * l + c] = __float2bfloat16_rn(y);
-                    } else if (c < kOut && out && valid) {
-                        out[size_t(s) * kOut + c] = v[j] + sm.bias[bias_o + c];
+                for (int q = 0; q < 4; ++q) {
+                    float y[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) y[j] = fmaxf(v[8 * q + j] + sm.bias[bias_o + c0 + 8 * q + j], 0.f);
+                    const uint4 u = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]),
+                                               pack_bf16x2(y[4], y[5]), pack_bf16x2(y[6], y[7]));
+                    *reinterpret_cast<uint4*>(sm.act + tc::kmajor_offset(row, c0 + 8 * q, kHidden)) = u;
+                    if (act_row) act_row[10 + 8 * l + half * 4 + q] = u;
+                }
+            } else if (half == 0) {
+                float v[32];
+                tc::tmem_ld16(tmem + lane_base, v);
+                tc::tmem_ld16(tmem + lane_base + 16u, v + 16);
+                if (out && valid) {
+                    float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        o4[q] = make_float4(v[4 * q] + sm.bias[bias_o + 4 * q], v[4 * q + 1] + sm.bias[bias_o + 4 * q + 1],
+                                            v[4 * q + 2] + sm.bias[bias_o + 4 * q + 2],
+                                            v[4 * q + 3] + sm.bias[bias_o + 4 * q + 3]);
+                    }
+                }
+            } else {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base + 32u, v);
+                if (out && valid) {
+                    float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut + 32);
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        o4[q] = make_float4(v[4 * q] + sm.bias[bias_o + 32 + 4 * q],
+                                            v[4 * q + 1] + sm.bias[bias_o + 32 + 4 * q + 1],
+                                            v[4 * q + 2] + sm.bias[bias_o + 32 + 4 * q + 2],
+                                            v[4 * q + 3] + sm.bias[bias_o + 32 + 4 * q + 3]);
                     }
                 }
             }
@@ -164,9 +223,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_mlp_forward(uint32_t n, const u
             tc::tc_fence_before_sync();
             __syncthreads();
             tc::tc_fence_after_sync();
-            uint8_t* t = in;
-            in = outb;
-            outb = t;
         }
     }
     if (sm.abort && tid == 0) {
@@ -231,7 +287,8 @@ __device__ __forceinline__ float head_grad(const float raw[kOut], const float di
 
 // features/acts/out as produced by k_mlp_forward for the same samples;
 // dirs: n x 3 unit directions; weight: n target weights c. grad += dLoss/dparams.
-__global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const __nv_bfloat16* __restrict__ acts,
+__global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const uint32_t* __restrict__ n_dev,
+                                                              const __nv_bfloat16* __restrict__ acts,
                                                               const float* __restrict__ out,
                                                               const float* __restrict__ dirs,
                                                               const float* __restrict__ weight, Weights wts,
@@ -240,6 +297,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const 
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    if (n_dev) n = min(n, *n_dev);
     for (int i = tid; i < kBwdBytes / 16; i += kThreads) {
         reinterpret_cast<uint4*>(sm.wt)[i] = reinterpret_cast<const uint4*>(wts.bwd)[i];
     }
@@ -349,11 +407,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const 
 }
 
 // ------------------------------------------------------------ Adam + pack
+// Per-step training state, resident on the device so that a training step
+// needs no host synchronisation: the sample count may come from a device
+// counter (the records of a render pass).
+struct TrainState {
+    uint32_t n;        // samples of this step
+    int32_t skip;      // fewer than the step's minimum: no update
+    uint32_t step;     // Adam steps taken
+    float bc1, bc2;    // bias corrections of this step
+    float scale;       // 1 / n (the loss is a mean over samples)
+    float loss_mean;   // loss of the last step / n
+};
+
+__global__ void k_train_prep(const uint32_t* __restrict__ n_dev, uint32_t n, uint32_t min_n, TrainState* s, float b1,
+                             float b2) {
+    if (n_dev) n = min(n, *n_dev);
+    s->n = n;
+    s->skip = n < min_n ? 1 : 0;
+    if (s->skip) return;
+    s->step += 1;
+    s->bc1 = 1.f - powf(b1, static_cast<float>(s->step));
+    s->bc2 = 1.f - powf(b2, static_cast<float>(s->step));
+    s->scale = 1.f / static_cast<float>(n);
+}
+
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
-                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float scale,
-                       float bc1, float bc2) {
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps, TrainState* s,
+                       const float* __restrict__ loss_sum) {
+    if (s->skip) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) s->loss_mean = *loss_sum * s->scale;
     if (i >= n) return;
+    const float scale = s->scale, bc1 = s->bc1, bc2 = s->bc2;
     const float gi = g[i] * scale;
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
@@ -399,7 +484,7 @@ struct turner_guide {
     uint8_t* bwd = nullptr;
     float* loss = nullptr;
     int* err = nullptr;
-    uint64_t step = 0;
+    TrainState* state = nullptr;
     // training-batch scratch, grown on demand
     size_t cap = 0;
     float* feat = nullptr;
@@ -459,9 +544,9 @@ unsigned grid_tiles(turner_guide* g, uint32_t n) {
     return std::max(1u, std::min<unsigned>(static_cast<unsigned>(g->sms), (n + 127) / 128));
 }
 
-// Two forward CTAs per SM: one's MMAs overlap the other's epilogue.
+// Three forward CTAs per SM: one's MMAs overlap the others' epilogues.
 unsigned grid_tiles_fwd(turner_guide* g, uint32_t n) {
-    return std::max(1u, std::min<unsigned>(2u * static_cast<unsigned>(g->sms), (n + 127) / 128));
+    return std::max(1u, std::min<unsigned>(kFwdBlocksPerSm * static_cast<unsigned>(g->sms), (n + 127) / 128));
 }
 
 } // namespace
@@ -473,7 +558,7 @@ namespace guide {
 int forward_device(turner_guide* g, const float* feat, uint32_t n, float* out, cudaStream_t stream) {
     if (n == 0) return TURNER_OK;
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles_fwd(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, out, nullptr, g->err);
+    k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, out, nullptr, g->err);
     return cuda_status(cudaGetLastError());
 }
 
@@ -482,7 +567,7 @@ int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uin
                   cudaStream_t stream) {
     if (cap == 0) return TURNER_OK;
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles_fwd(g, cap), kThreads, fwd_smem(), stream>>>(cap, n_dev, feat, w, out, nullptr, g->err);
+    k_mlp_forward<<<grid_tiles_fwd(g, cap), kFwdThreads, fwd_smem(), stream>>>(cap, n_dev, feat, w, out, nullptr, g->err);
     return cuda_status(cudaGetLastError());
 }
 
@@ -514,32 +599,41 @@ int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const
 
 // One Adam step on n device-resident samples (features n x 9, dirs n x 3,
 // weights n); optional loss (mean of -c log q) copied out.
-int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n, float lr,
-                 cudaStream_t stream, float* loss_out) {
+int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n,
+                 const uint32_t* n_dev, uint32_t min_n, float lr, cudaStream_t stream, float* loss_out) {
     if (n == 0) return TURNER_OK;
     int st = ensure_batch(g, n);
     if (st != TURNER_OK) return st;
     Weights w{g->fwd, g->bwd, g->params};
+    const float b1 = 0.9f, b2 = 0.999f;
     GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), stream));
     GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), stream));
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), stream>>>(n, nullptr, feat, w, g->out, g->acts, g->err);
-    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), stream>>>(n, g->acts, g->out, dirs, wts, w, g->grad,
-                                                                      g->loss, g->err);
-    g->step += 1;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float bc1 = 1.f - std::pow(b1, static_cast<float>(g->step));
-    const float bc2 = 1.f - std::pow(b2, static_cast<float>(g->step));
+    k_train_prep<<<1, 1, 0, stream>>>(n_dev, n, min_n, g->state, b1, b2);
+    const uint32_t* n_step = &g->state->n;
+    k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), stream>>>(n, n_step, feat, w, g->out, g->acts,
+                                                                             g->err);
+    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), stream>>>(n, n_step, g->acts, g->out, dirs, wts, w,
+                                                                      g->grad, g->loss, g->err);
     k_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->params, g->grad, g->m, g->v, kParams, lr, b1, b2, 1e-8f,
-                                                      1.f / static_cast<float>(n), bc1, bc2);
+                                                      g->state, g->loss);
     k_pack<<<dim3(16, kLayers), 256, 0, stream>>>(g->params, g->fwd, g->bwd);
     GCK(cudaGetLastError());
     g->train_steps += 1;
     if (loss_out) {
-        float l = 0;
-        GCK(cudaMemcpyAsync(&l, g->loss, sizeof(float), cudaMemcpyDeviceToHost, stream));
+        TrainState s{};
+        GCK(cudaMemcpyAsync(&s, g->state, sizeof(s), cudaMemcpyDeviceToHost, stream));
         GCK(cudaStreamSynchronize(stream));
-        *loss_out = l / static_cast<float>(n);
+        *loss_out = s.loss_mean;
     }
+    return TURNER_OK;
+}
+
+int train_state(turner_guide* g, uint64_t* steps, float* last_loss) {
+    TrainState s{};
+    GCK(cudaMemcpyAsync(&s, g->state, sizeof(s), cudaMemcpyDeviceToHost, g->stream));
+    GCK(cudaStreamSynchronize(g->stream));
+    if (steps) *steps = s.step;
+    if (last_loss) *last_loss = s.loss_mean;
     return TURNER_OK;
 }
 
@@ -572,6 +666,7 @@ int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
     if (e == cudaSuccess) e = cudaMalloc(&g->bwd, kBwdBytes);
     if (e == cudaSuccess) e = cudaMalloc(&g->loss, sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&g->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&g->state, sizeof(TrainState));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    static_cast<int>(fwd_smem()));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -606,6 +701,7 @@ int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
     if (e == cudaSuccess) e = cudaMemset(g->m, 0, kParams * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(g->v, 0, kParams * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(g->state, 0, sizeof(TrainState));
     if (e == cudaSuccess) {
         k_pack<<<dim3(16, kLayers), 256, 0, g->stream>>>(g->params, g->fwd, g->bwd);
         e = cudaStreamSynchronize(g->stream);
@@ -626,7 +722,7 @@ void turner_guide_destroy(turner_guide* g) {
                     static_cast<void*>(g->grad), static_cast<void*>(g->fwd), static_cast<void*>(g->bwd),
                     static_cast<void*>(g->loss), static_cast<void*>(g->err), static_cast<void*>(g->feat),
                     static_cast<void*>(g->dirs), static_cast<void*>(g->wts), static_cast<void*>(g->out),
-                    static_cast<void*>(g->acts)}) {
+                    static_cast<void*>(g->acts), static_cast<void*>(g->state)}) {
         if (p) cudaFree(p);
     }
     delete g;
@@ -672,9 +768,9 @@ int turner_guide_gradient(turner_guide* g, const float* features, const float* d
     GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), g->stream));
     GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), g->stream));
     Weights w{g->fwd, g->bwd, g->params};
-    k_mlp_forward<<<grid_tiles(g, n), kThreads, fwd_smem(), g->stream>>>(n, nullptr, g->feat, w, g->out, g->acts, g->err);
-    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), g->stream>>>(n, g->acts, g->out, g->dirs, g->wts, w,
-                                                                         g->grad, g->loss, g->err);
+    k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), g->stream>>>(n, nullptr, g->feat, w, g->out, g->acts, g->err);
+    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), g->stream>>>(n, nullptr, g->acts, g->out, g->dirs,
+                                                                         g->wts, w, g->grad, g->loss, g->err);
     GCK(cudaGetLastError());
     GCK(cudaMemcpyAsync(grad_out, g->grad, kParams * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     float l = 0;
@@ -695,7 +791,8 @@ int turner_guide_train(turner_guide* g, const float* features, const float* dirs
     GCK(cudaMemcpyAsync(g->wts, weights, n * sizeof(float), cudaMemcpyHostToDevice, g->stream));
     float loss = 0;
     for (uint32_t i = 0; i < steps; ++i) {
-        st = guide::train_device(g, g->feat, g->dirs, g->wts, n, lr, g->stream, i + 1 == steps ? &loss : nullptr);
+        st = guide::train_device(g, g->feat, g->dirs, g->wts, n, nullptr, 1, lr, g->stream,
+                                 i + 1 == steps ? &loss : nullptr);
         if (st != TURNER_OK) return st;
     }
     if (loss_out) *loss_out = loss;

@@ -131,7 +131,12 @@ int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uin
 int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const uint32_t* path,
                      const float* l_before, const float* t_after, const float* fcos_pdf, float* weight,
                      cudaStream_t stream);
-int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n, float lr,
-                 cudaStream_t stream, float* loss_out);
+// One Adam step on n samples, or on min(n, *n_dev) when n_dev is given; a
+// step with fewer than min_n samples changes nothing. Asynchronous unless
+// loss_out is given (then it waits and writes the step's mean loss).
+int train_device(turner_guide* g, const float* feat, const float* dirs, const float* wts, uint32_t n,
+                 const uint32_t* n_dev, uint32_t min_n, float lr, cudaStream_t stream, float* loss_out);
+// Adam steps taken and the last step's mean loss (waits for the stream).
+int train_state(turner_guide* g, uint64_t* steps, float* last_loss);
 } // namespace guide
 } // namespace turner
