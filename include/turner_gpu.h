@@ -252,7 +252,10 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
  *   chunk_paths    paths in flight per render pass (queue length)
  *   mailbox        1: skip a triangle this ray tested in the last four tests
  *                  (exact: a repeat cannot change the answer; 128-thread blocks)
- *   min_blocks     12: cap traversal registers so 12 blocks fit per SM, 0: no cap */
+ *   min_blocks     10, 12 or 16: cap traversal registers so that many 128-thread
+ *                  blocks fit per SM (48, 40, 32 registers), 0: no cap.
+ *                  Default 12: the traversal is latency-bound and 12 blocks
+ *                  beat the uncapped 9 despite a few spilled registers */
 typedef struct turner_tuning {
     int32_t persistent;
     uint32_t blocks_per_sm;

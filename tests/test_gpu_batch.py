@@ -129,6 +129,7 @@ def test_autotune_caches_and_keeps_images(ctx, scenes, tmp_path, monkeypatch):
     """The tuner times launch shapes on the batch, applies the fastest and
     caches it per GPU and batch shape; any tuned shape renders the same image."""
     monkeypatch.setenv("TURNER_TUNE_CACHE", str(tmp_path / "tuning.txt"))
+    default = ctx.get_tuning()
     jobs = make_jobs(scenes)[:3]
     before, _ = ctx.render(jobs)
     t = ctx.autotune(jobs, force=True)
@@ -149,7 +150,7 @@ def test_autotune_caches_and_keeps_images(ctx, scenes, tmp_path, monkeypatch):
         again, _ = ctx.render(jobs)
         for a, b in zip(before, again):
             assert np.array_equal(a, b)
-    ctx.set_tuning(tg.Tuning(1, 0, 128, 128, 1 << 24, 0, 0, 0.0, 0))
+    ctx.set_tuning(default)
 
 
 def test_too_many_jobs_rejected(ctx, scenes):

@@ -86,10 +86,12 @@ def test_launch_shapes_agree(ctx, uploaded, persistent, blocks):
 
 
 @pytest.mark.parametrize("block,stack,mailbox,min_blocks", [(128, 128, 1, 0), (128, 64, 1, 12), (256, 64, 0, 0),
-                                                           (128, 128, 0, 12)])
+                                                           (128, 128, 0, 12), (128, 64, 0, 10), (128, 128, 0, 16),
+                                                           (128, 128, 1, 16), (128, 128, 0, 0)])
 def test_tuned_shapes_agree(ctx, uploaded, block, stack, mailbox, min_blocks):
     """Every tuning variant (block size, stack depth, triangle mailbox,
     register cap) returns the same bit-exact closest hits."""
+    default = ctx.get_tuning()
     for name in ("sphere5", "soup20k"):
         sid, ref, box = uploaded[name]
         o, d = tg.make_rays(150_000, box, seed=41)
@@ -98,7 +100,7 @@ def test_tuned_shapes_agree(ctx, uploaded, block, stack, mailbox, min_blocks):
             gpu = ctx.intersect(sid, o, d)
             fast = ctx.intersect(sid, o, d, mode=tg.TRAVERSAL_FAST)
         finally:
-            ctx.set_tuning(tg.Tuning(1, 0, 128, 128, 1 << 24, 0, 0, 0.0, 0))
+            ctx.set_tuning(default)
         cpu = ref.intersect(o, d)
         assert_same(gpu, cpu)
         assert np.array_equal(fast[0], cpu[0])

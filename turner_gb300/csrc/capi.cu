@@ -853,13 +853,15 @@ void tuning_store(const std::string& key, const turner_tuning& t) {
     std::fclose(f);
 }
 
+bool valid_min_blocks(uint32_t v) { return v == 0 || v == 10 || v == 12 || v == 16; }
+
 void apply_tuning(turner_ctx* ctx, const turner_tuning& t) {
     ctx->traverse.persistent = t.persistent != 0;
     ctx->traverse.blocks_per_sm = t.blocks_per_sm;
     ctx->traverse.block = t.block == 256 ? 256 : 128;
     ctx->traverse.stack = t.stack == 64 ? 64 : kStackCap;
     ctx->traverse.mailbox = t.mailbox != 0;
-    ctx->traverse.min_blocks = t.min_blocks == 12 ? 12 : 0;
+    ctx->traverse.min_blocks = valid_min_blocks(t.min_blocks) ? t.min_blocks : 0;
     ctx->chunk_paths = std::max<uint32_t>(1024, t.chunk_paths);
 }
 
@@ -870,7 +872,7 @@ extern "C" {
 int turner_set_tuning(turner_ctx* ctx, const turner_tuning* t) {
     if (!ctx || !t) return TURNER_ERR_INVALID_ARG;
     if ((t->block != 128 && t->block != 256) || (t->stack != 64 && t->stack != kStackCap) || t->blocks_per_sm > 64 ||
-        t->chunk_paths < 1024 || t->mailbox > 1 || (t->min_blocks != 0 && t->min_blocks != 12))
+        t->chunk_paths < 1024 || t->mailbox > 1 || !valid_min_blocks(t->min_blocks))
         return TURNER_ERR_INVALID_ARG;
     apply_tuning(ctx, *t);
     return TURNER_OK;
@@ -934,7 +936,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
         return TURNER_OK;
     };
     // coordinate descent from the defaults, one knob at a time
-    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 0, 0, 0};
+    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 12, 0, 0};
     int s = measure(cur, cur.ms);
     if (s != TURNER_OK) return s;
     const uint32_t blocks[] = {128, 256};
@@ -982,7 +984,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
                 if (t.min_blocks == v || t.block != 128) return false;
                 t.min_blocks = v;
                 return true;
-            }, std::vector<uint32_t>{12});
+            }, std::vector<uint32_t>{0, 10, 16});
     if (s == TURNER_OK)
         s = try_value([&](turner_tuning& t, int v) { if (t.persistent == v) return false; t.persistent = v; return true; },
                       std::vector<int>{0});

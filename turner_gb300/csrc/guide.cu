@@ -139,21 +139,25 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
     uint32_t phase = 0;
     const uint32_t tiles = (n + 127) / 128;
 
+    // this row's 9 input floats; the next tile's are loaded while the
+    // current tile runs through the layers
+    float fin[9];
+    auto load_features = [&](uint32_t t) {
+        const uint32_t s = t * 128 + row;
+        if (t < tiles && s < n) {
+            const float* q = features + 9 * size_t(s);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) fin[k] = q[k];
+        }
+    };
+    load_features(blockIdx.x);
     for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
         const uint32_t s = tile * 128 + row;
         const bool valid = s < n;
         uint4* const act_row = acts && valid ? reinterpret_cast<uint4*>(acts + size_t(s) * 336) : nullptr;
         {
-            float p[3] = {0.f, 0.f, 0.f}, nn[3] = {0.f, 0.f, 0.f}, a[3] = {0.f, 0.f, 0.f};
-            if (valid) {
-                const float* q = features + 9 * size_t(s);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    p[k] = q[k];
-                    nn[k] = q[3 + k];
-                    a[k] = q[6 + k];
-                }
-            }
+            const float p[3] = {fin[0], fin[1], fin[2]}, nn[3] = {fin[3], fin[4], fin[5]},
+                        a[3] = {fin[6], fin[7], fin[8]};
 #pragma unroll 1
             for (int g = half * 5; g < half * 5 + 5; ++g) {
                 const uint4 v = valid ? encode_group(g, p, nn, a) : make_uint4(0u, 0u, 0u, 0u);
@@ -161,6 +165,7 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
                 if (act_row) act_row[g] = v;
             }
         }
+        load_features(tile + gridDim.x);
         tc::fence_async_smem();
         tc::tc_fence_before_sync();
         __syncthreads();

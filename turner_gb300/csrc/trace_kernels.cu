@@ -17,6 +17,8 @@
 // cosine bounce). This is the reference's recursion
 // L_k = diffuse * (direct / pi + 2 cos L_{k+1}) unrolled.
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "device.cuh"
 #include "guide.cuh"
@@ -417,9 +419,9 @@ struct SoaSrc {             // turner_intersect batches
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
 // while rays of very different lengths are traversed. MULTI: every ray names
 // its job and is traced in that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
-                                                           uint32_t* __restrict__ work) {
+template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX>
+__device__ __forceinline__ void traverse_persistent(const SceneView& single, const JobDesc* __restrict__ jobs,
+                                                    Src& src, uint32_t* __restrict__ work) {
     const uint32_t n = src.count();
     uint32_t st_node[STACK];
     float st_enter[STACK], st_exit[STACK];
@@ -460,6 +462,22 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_traverse(SceneView single, cons
             active = false;
         }
     }
+}
+
+// Two kernels over the same body: naming a minimum of one resident block in
+// __launch_bounds__ changes ptxas's register budget (61 instead of 56
+// registers for the closest-hit kernel, 8 instead of 9 resident blocks), so
+// the uncapped kernel gives only the block size.
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX>
+__global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
+                                                     uint32_t* __restrict__ work) {
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work);
+}
+
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_traverse_capped(SceneView single, const JobDesc* __restrict__ jobs,
+                                                                  Src src, uint32_t* __restrict__ work) {
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work);
 }
 
 // Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
@@ -515,23 +533,35 @@ inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock 
 
 // Resident blocks per SM x SMs for a persistent kernel (cached per kernel).
 template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap) {
-    static int sms = 0, per_sm = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, 0);
-        sms = std::max(1, sms);
-        per_sm = std::max(1, per_sm);
+    // resident blocks per SM, per kernel (kernels that share a signature
+    // differ in registers) and per device
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, std::pair<int, int>> cache;   // -> (SMs, blocks per SM)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::pair<int, int> v;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto key = std::make_pair(reinterpret_cast<const void*>(kernel), dev);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            int sms = 0, per_sm = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, 0);
+            it = cache.emplace(key, std::make_pair(std::max(1, sms), std::max(1, per_sm))).first;
+        }
+        v = it->second;
     }
-    const unsigned per = blocks_per_sm_cap ? std::min<unsigned>(per_sm, blocks_per_sm_cap) : per_sm;
-    return static_cast<unsigned>(sms) * per;
+    const unsigned per = blocks_per_sm_cap ? std::min<unsigned>(v.second, blocks_per_sm_cap) : v.second;
+    return static_cast<unsigned>(v.first) * per;
 }
 
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
 void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
                         const TraverseCfg& cfg, cudaStream_t stream) {
-    auto kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB>;
+    void (*kernel)(SceneView, const JobDesc*, Src, uint32_t*);
+    if constexpr (MINB > 1) kernel = k_traverse_capped<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB>;
+    else kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX>;
     const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
     const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm), std::max(1u, need));
     kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work);
@@ -553,17 +583,22 @@ void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, 
         }
         return;
     }
-    // 128-thread blocks: mailbox on/off x register cap for 12 resident blocks on/off
+    // 128-thread blocks: mailbox on/off x register cap for 10, 12 or 16 resident blocks (or none)
 #define TURNER_SHAPE(ST, MB, MINB) \
     run_traverse_shape<Src, ANY, FAST, MULTI, 128, ST, MB, MINB>(single, jobs, src, capacity, cfg, stream)
-    const bool mb = cfg.mailbox, occ = cfg.min_blocks == 12;
-    if (small_stack) {
-        if (mb) { if (occ) TURNER_SHAPE(64, true, 12); else TURNER_SHAPE(64, true, 1); }
-        else { if (occ) TURNER_SHAPE(64, false, 12); else TURNER_SHAPE(64, false, 1); }
-    } else {
-        if (mb) { if (occ) TURNER_SHAPE(kStackCap, true, 12); else TURNER_SHAPE(kStackCap, true, 1); }
-        else { if (occ) TURNER_SHAPE(kStackCap, false, 12); else TURNER_SHAPE(kStackCap, false, 1); }
+#define TURNER_CAPS(ST, MB)                               \
+    switch (cfg.min_blocks) {                             \
+    case 10: TURNER_SHAPE(ST, MB, 10); break;             \
+    case 12: TURNER_SHAPE(ST, MB, 12); break;             \
+    case 16: TURNER_SHAPE(ST, MB, 16); break;             \
+    default: TURNER_SHAPE(ST, MB, 1); break;              \
     }
+    if (small_stack) {
+        if (cfg.mailbox) { TURNER_CAPS(64, true) } else { TURNER_CAPS(64, false) }
+    } else {
+        if (cfg.mailbox) { TURNER_CAPS(kStackCap, true) } else { TURNER_CAPS(kStackCap, false) }
+    }
+#undef TURNER_CAPS
 #undef TURNER_SHAPE
 }
 
