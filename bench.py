@@ -302,6 +302,131 @@ def run_guide(args) -> None:
     ctx.close()
 
 
+def run_views16(args) -> None:
+    """Learned proposal + batching: the 327,680-triangle displaced icosphere
+    inside the baffled room (wall tessellation 64 per side), 16 camera views
+    on a circle around the sphere at height 1.5 (radius --views-radius),
+    1920x1080 each, max depth 5, one batch per render call (one CUDA graph when
+    not training). One shared proposal is trained online across all views,
+    then the guided and the cosine tracer each render --views-spp samples per
+    view. Also an equal-time MSE comparison at 320x180 per view against an
+    FP64-accumulated cosine reference (host-side sums of linear renders)."""
+    import torch
+
+    import turner_gb300 as tg
+
+    ctx = tg.Context(0)
+    t0 = time.perf_counter()
+    mesh = tg.make_scene(tg.SCENE_BAFFLE_SPHERE, detail=7, count=64, aspect=16 / 9)
+    sid = ctx.upload_tree(tg.KDTree.from_mesh(mesh))
+    build_s = time.perf_counter() - t0
+    center = (2.78, 1.65, -3.5)
+    cams = []
+    for k in range(16):
+        a = 2 * np.pi * k / 16
+        pos = (center[0] + args.views_radius * np.cos(a), 1.5, center[2] + args.views_radius * np.sin(a))
+        cams.append(tg.look_at_camera(pos, center, 16 / 9))
+
+    def jobs(w, h, spp, sampling, seed):
+        out = []
+        for k, cam in enumerate(cams):
+            j = tg.make_job(sid, mesh, w, h, pixel_samples=spp, max_depth=5, seed=seed * 131 + k, sampling=sampling)
+            j.camera = cam
+            j.linear_output = 1
+            out.append(j)
+        return out
+
+    W, H = 1920, 1080
+    outs = [torch.empty((H, W, 4), dtype=torch.float32, device="cuda") for _ in cams]
+    ptrs = [o.data_ptr() for o in outs]
+    guide = tg.Guide(ctx, seed=11)
+    ctx.set_guide(guide, train=True, lr=args.guide_lr, records=args.guide_records, steps_per_pass=args.guide_steps)
+    t = time.perf_counter()
+    calls = 0
+    while time.perf_counter() - t < args.views_train_s:
+        ctx.render(jobs(W, H, 1, tg.SAMPLING_GUIDED, 1000 + calls), ptrs, tg.DEVICE_BUFFERS)
+        calls += 1
+    train_wall = time.perf_counter() - t
+    steps, loss, train_ms = ctx.guide_stats()
+    ctx.set_guide(guide, train=False)
+    thr = {}
+    for name, sampling in (("guided", tg.SAMPLING_GUIDED), ("cosine", tg.SAMPLING_COSINE)):
+        ctx.render(jobs(W, H, 1, sampling, 7), ptrs, tg.DEVICE_BUFFERS)   # workspace, graph shapes
+        torch.cuda.synchronize()
+        g0 = ctx.graph_launch_count()
+        _, stats = ctx.render(jobs(W, H, args.views_spp, sampling, 11), ptrs, tg.DEVICE_BUFFERS)
+        rays = sum(st.rays for st in stats)
+        ctx.set_profiling(True)
+        ctx.set_graph_mode(tg.GRAPH_NEVER)   # per-kernel events need uncaptured launches
+        ctx.kernel_times(reset=True)
+        ctx.render(jobs(W, H, 2, sampling, 13), ptrs, tg.DEVICE_BUFFERS)
+        kt = ctx.kernel_times(reset=True)
+        ctx.set_graph_mode(tg.GRAPH_AUTO)
+        ctx.set_profiling(False)
+        total = sum(v[0] for v in kt.values())
+        thr[name] = {"mrays_per_s": round(rays / stats[0].device_ms / 1e3, 2), "ms": round(stats[0].device_ms, 1),
+                     "rays": int(rays), "graph_launches": ctx.graph_launch_count() - g0,
+                     "kernel_share": {k: round(v[0] / total, 4) for k, v in kt.items() if v[1]}}
+
+    # equal-time MSE at 320x180 per view
+    w, h = 320, 180
+    small = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for _ in cams]
+    sptr = [o.data_ptr() for o in small]
+
+    def accumulate(sampling, spp, seed, calls=None, budget=None, train_fraction=0.0):
+        acc = np.zeros((16, h, w, 3))
+        n, t = 0, time.perf_counter()
+        training = train_fraction > 0
+        while (calls is not None and n < calls) or (budget is not None and time.perf_counter() - t < budget):
+            if training and time.perf_counter() - t > train_fraction * budget:
+                ctx.set_guide(ctx_guide[0], train=False)
+                training = False
+            ctx.render(jobs(w, h, spp, sampling, seed + n), sptr, tg.DEVICE_BUFFERS)
+            acc += np.stack([o[..., :3].cpu().numpy() for o in small])
+            n += 1
+        return acc / n, n * spp, time.perf_counter() - t
+
+    ctx_guide = [None]
+    t0 = time.perf_counter()
+    half = max(1, args.views_ref_spp // 128)
+    ref_a, _, _ = accumulate(tg.SAMPLING_COSINE, 64, 500000, calls=half)
+    ref_b, _, _ = accumulate(tg.SAMPLING_COSINE, 64, 600000, calls=half)
+    ref_s = time.perf_counter() - t0
+    ref = 0.5 * (ref_a + ref_b)
+    ref_var = float(((ref_a - ref_b) ** 2).mean() / 4)
+    plain, plain_spp, plain_s = accumulate(tg.SAMPLING_COSINE, args.pass_spp, 7, budget=args.budget)
+    g2 = tg.Guide(ctx, seed=12)
+    ctx_guide[0] = g2
+    ctx.set_guide(g2, train=False)
+    ctx.render(jobs(w, h, args.pass_spp, tg.SAMPLING_GUIDED, 3), sptr, tg.DEVICE_BUFFERS)   # workspace
+    ctx.set_guide(g2, train=True, lr=args.guide_lr, records=args.guide_records, steps_per_pass=args.guide_steps)
+    learned, learned_spp, learned_s = accumulate(tg.SAMPLING_GUIDED, args.pass_spp, 7, budget=args.budget,
+                                                 train_fraction=args.train_fraction)
+    ctx.set_guide(None)
+    m_plain = float(((plain - ref) ** 2).mean())
+    m_learned = float(((learned - ref) ** 2).mean())
+    print(json.dumps({
+        "metric": "Mrays/s, 16 views with the online-trained learned proposal (reference ray count)",
+        "value": thr["guided"]["mrays_per_s"], "unit": "Mrays/s", "higher_is_better": True, "n_gpus": 1,
+        "dtype": "bf16 MLP / f32 tracing", "data": "synthetic",
+        "config": {"workload": f"baffled room + displaced icosphere, 16 views 1920x1080 x {args.views_spp} spp, depth 5",
+                   "triangles": int(mesh.n_triangles), "views_radius": args.views_radius,
+                   "host_tree_build_s": round(build_s, 2)},
+        "guided": thr["guided"], "cosine": thr["cosine"],
+        "training": {"calls": calls, "wall_s": round(train_wall, 2), "adam_steps": int(steps),
+                     "last_loss": round(loss, 4), "train_ms": round(train_ms, 1)},
+        "equal_time": {"views": "16 x 320x180", "budget_s": args.budget, "reference_spp": 2 * half * 64,
+                       "reference_s": round(ref_s, 1), "reference_variance": ref_var,
+                       "plain": {"mse": m_plain, "spp": plain_spp, "wall_s": round(plain_s, 2)},
+                       "learned": {"mse": m_learned, "spp": learned_spp, "wall_s": round(learned_s, 2)},
+                       "mse_ratio": round(m_plain / m_learned, 4),
+                       "mse_ratio_reference_noise_removed": round((m_plain - ref_var) / (m_learned - ref_var), 4)},
+    }))
+    guide.close()
+    g2.close()
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -315,7 +440,11 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="480x270 frame of the same scene (for profiler captures; not a bench line)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch64", "guide"])
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch64", "guide", "views16"])
+    ap.add_argument("--views-radius", type=float, default=4.0)
+    ap.add_argument("--views-spp", type=int, default=64)
+    ap.add_argument("--views-train-s", type=float, default=3.0)
+    ap.add_argument("--views-ref-spp", type=int, default=2048)
     ap.add_argument("--guide-side", type=int, default=512)
     ap.add_argument("--ref-spp", type=int, default=8192)
     ap.add_argument("--pass-spp", type=int, default=4)
@@ -333,6 +462,9 @@ def main() -> None:
         return
     if args.workload == "guide":
         run_guide(args)
+        return
+    if args.workload == "views16":
+        run_views16(args)
         return
     if args.small:
         global WIDTH, HEIGHT, WORKLOAD

@@ -276,9 +276,16 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
 int turner_set_tuning(turner_ctx* ctx, const turner_tuning* tuning);
 int turner_get_tuning(turner_ctx* ctx, turner_tuning* tuning);
 
-/* Capture single-job renders into a CUDA graph too (always != 0). No
- * reference counterpart. */
-int turner_set_graph_mode(turner_ctx* ctx, int always);
+/* When renders are captured into a CUDA graph. AUTO (default): batches of
+ * more than one job; ALWAYS: every render and accumulate pass; NEVER: no
+ * capture (per-kernel timing with turner_set_profiling needs it). A batch of
+ * the same shape as the previous one updates the instantiated graph in place
+ * (cudaGraphExecUpdate) instead of instantiating a new one. Renders that
+ * train the learned proposal are never captured. No reference counterpart. */
+#define TURNER_GRAPH_AUTO 0
+#define TURNER_GRAPH_ALWAYS 1
+#define TURNER_GRAPH_NEVER 2
+int turner_set_graph_mode(turner_ctx* ctx, int mode);
 /* Number of CUDA graphs launched by this context. No reference counterpart. */
 uint64_t turner_graph_launch_count(turner_ctx* ctx);
 

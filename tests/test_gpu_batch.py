@@ -93,6 +93,30 @@ def test_graph_mode_single_job(ctx, scenes):
     assert np.array_equal(a, b)
 
 
+def test_graph_reuse_across_batches(ctx, scenes):
+    """Batches of the same shape update the instantiated graph in place; the
+    images equal uncaptured renders, also after a batch of another shape."""
+    import copy
+    jobs = make_jobs(scenes)
+    reseeded = [copy.copy(j) for j in jobs]
+    for j in reseeded:
+        j.seed += 1000
+    a, _ = ctx.render(jobs)
+    b, _ = ctx.render(reseeded)
+    ctx.render(jobs[:3])                      # another topology in between
+    c, _ = ctx.render(jobs)
+    ctx.set_graph_mode(tg.GRAPH_NEVER)
+    try:
+        d, _ = ctx.render(reseeded)
+    finally:
+        ctx.set_graph_mode(tg.GRAPH_AUTO)
+    assert all(np.array_equal(x, y) for x, y in zip(a, c))
+    assert all(np.array_equal(x, y) for x, y in zip(b, d))
+    assert not all(np.array_equal(x, y) for x, y in zip(a, b))
+    with pytest.raises(tg.TurnerError):
+        ctx.set_graph_mode(7)
+
+
 def test_linear_output_matches_oracle(ctx, scenes):
     m, sid, ref = scenes["room"]
     job = tg.make_job(sid, m, 32, 32, pixel_samples=4, max_depth=3, seed=21)

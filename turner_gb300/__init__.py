@@ -49,6 +49,7 @@ SCENE_BAFFLE_SPHERE = 4
 
 TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
+GRAPH_AUTO, GRAPH_ALWAYS, GRAPH_NEVER = 0, 1, 2
 KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect", "k_guide_features",
                 "k_mlp_forward", "guide_train")
 KERNEL_KINDS = len(KERNEL_NAMES)
@@ -378,8 +379,10 @@ class Context:
         _check(_lib().turner_guide_stats(self._h, C.byref(steps), C.byref(loss), C.byref(ms)), "turner_guide_stats")
         return steps.value, loss.value, ms.value
 
-    def set_graph_mode(self, always: bool) -> None:
-        _check(_lib().turner_set_graph_mode(self._h, 1 if always else 0), "turner_set_graph_mode")
+    def set_graph_mode(self, mode) -> None:
+        """True / GRAPH_ALWAYS, False / GRAPH_AUTO, or GRAPH_NEVER."""
+        m = GRAPH_ALWAYS if mode is True else GRAPH_AUTO if mode is False else int(mode)
+        _check(_lib().turner_set_graph_mode(self._h, m), "turner_set_graph_mode")
 
     def graph_launch_count(self) -> int:
         return _lib().turner_graph_launch_count(self._h)
@@ -464,6 +467,27 @@ class Guide:
         _check(_lib().turner_guide_train(self._h, _ptr(f), _ptr(d), _ptr(w), f.shape[0], lr, steps, C.byref(loss)),
                "turner_guide_train")
         return loss.value
+
+
+def look_at_camera(position, target, aspect: float, vfov_deg: float = 40.0, up=(0.0, 1.0, 0.0)) -> Camera:
+    """Pinhole camera at `position` looking at `target` (lib/types.h:88-123
+    conventions: the camera looks down -z of its frame, so the rotation's
+    columns are right, up and -forward; delta_x = tan(vfov / 2) * aspect)."""
+    pos = np.asarray(position, np.float64)
+    f = np.asarray(target, np.float64) - pos
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    rot = np.stack([r, u, -f], axis=1)   # column-wise
+    cam = Camera()
+    for k in range(3):
+        cam.position[k] = pos[k]
+    for k, v in enumerate(rot.reshape(-1)):
+        cam.trafo[k] = v
+    cam.aspect = aspect
+    cam.delta_x = float(np.tan(np.radians(vfov_deg) / 2) * aspect)
+    return cam
 
 
 def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, pixel_samples: int = 1,

@@ -64,7 +64,9 @@ struct turner_ctx {
     DevBuf L, qa[4], qb[4], hits, shq[3], shjob, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
     uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
     uint64_t acc_samples = 0, acc_passes = 0;
-    bool use_graph = false;            // capture single-job renders too
+    int graph_mode = TURNER_GRAPH_AUTO;
+    cudaGraphExec_t graph_exec = nullptr;   // last instantiated batch graph, updated in place when it can be
+    uint64_t graph_updates = 0;
     // learned proposal used by jobs with TURNER_SAMPLING_GUIDED
     turner_guide* guide = nullptr;
     bool guide_train = false;
@@ -274,6 +276,7 @@ void turner_destroy(turner_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     ctx->scenes.clear();
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -671,10 +674,27 @@ int run_batch(turner_ctx* ctx, const Batch& b, double4* acc, turner_stats* stats
             return st;
         }
         TURNER_CK(ec);
-        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        // A batch of the same shape captures the same topology with new
+        // parameters: update the previous executable instead of
+        // instantiating a new one (instantiation costs milliseconds).
+        cudaError_t e = cudaSuccess;
+        if (ctx->graph_exec) {
+            cudaGraphExecUpdateResultInfo info{};
+            if (cudaGraphExecUpdate(ctx->graph_exec, graph, &info) == cudaSuccess) {
+                exec = ctx->graph_exec;
+                ctx->graph_updates += 1;
+            } else {
+                cudaGetLastError();   // clear the update's error; instantiate below
+                cudaGraphExecDestroy(ctx->graph_exec);
+                ctx->graph_exec = nullptr;
+            }
+        }
+        if (!exec) {
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            if (e == cudaSuccess) ctx->graph_exec = exec;
+        }
         if (e == cudaSuccess) e = cudaGraphLaunch(exec, ctx->stream);
         ctx->graph_launches += e == cudaSuccess ? 1 : 0;
-        if (exec) cudaGraphExecDestroy(exec);
         cudaGraphDestroy(graph);
         TURNER_CK(e);
     } else {
@@ -732,7 +752,8 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
     int st = plan_batch(ctx, jobs, n_jobs, outs.data(), true, b);
     if (st != TURNER_OK) return st;
     for (uint32_t j = 0; j < n_jobs; ++j) b.table[j].tone_map = jobs[j].linear_output ? 0 : 1;
-    st = run_batch(ctx, b, nullptr, stats, (n_jobs > 1 || ctx->use_graph) && !(b.guided && ctx->guide_train));
+    const bool graph = ctx->graph_mode == TURNER_GRAPH_ALWAYS || (ctx->graph_mode == TURNER_GRAPH_AUTO && n_jobs > 1);
+    st = run_batch(ctx, b, nullptr, stats, graph && !(b.guided && ctx->guide_train));
     if (st != TURNER_OK) return st;
     if (flags == TURNER_HOST_BUFFERS) {
         for (uint32_t j = 0; j < n_jobs; ++j) {
@@ -769,7 +790,8 @@ int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t pa
         Batch b;
         st = plan_batch(ctx, &jp, 1, nullptr, false, b);
         if (st != TURNER_OK) return st;
-        st = run_batch(ctx, b, ctx->acc.as<double4>(), nullptr, ctx->use_graph && !(b.guided && ctx->guide_train));
+        st = run_batch(ctx, b, ctx->acc.as<double4>(), nullptr,
+                       ctx->graph_mode == TURNER_GRAPH_ALWAYS && !(b.guided && ctx->guide_train));
         if (st != TURNER_OK) return st;
         ctx->acc_passes += 1;
         ctx->acc_samples += job->pixel_samples;
@@ -1024,9 +1046,10 @@ int turner_guide_stats(turner_ctx* ctx, uint64_t* steps, float* last_loss, doubl
     return TURNER_OK;
 }
 
-int turner_set_graph_mode(turner_ctx* ctx, int always) {
+int turner_set_graph_mode(turner_ctx* ctx, int mode) {
     if (!ctx) return TURNER_ERR_INVALID_ARG;
-    ctx->use_graph = always != 0;
+    if (mode < TURNER_GRAPH_AUTO || mode > TURNER_GRAPH_NEVER) return TURNER_ERR_INVALID_ARG;
+    ctx->graph_mode = mode;
     return TURNER_OK;
 }
 
