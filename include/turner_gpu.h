@@ -355,6 +355,35 @@ int turner_kdtree_export(const turner_kdtree* tree, uint64_t* nodes, turner_tria
 int turner_upload_kdtree(turner_ctx* ctx, const turner_kdtree* tree, uint32_t* scene_id);
 void turner_kdtree_free(turner_kdtree* tree);
 
+/* ---------------------------------------------------------- tree files */
+/* A binary file holding one kd-tree (node words, triangle records, box),
+ * keyed by the content of the triangles it was built from. Replaces the
+ * reference's fixed-name cereal cache ./kdtree.cache (main.cpp:142-167),
+ * which is not keyed by the scene. Layout: a 128-byte header ("TRNKDT01",
+ * key, counts, box, height, payload checksum), then the node words (8 bytes
+ * each), then the triangle records (192 bytes each), all little-endian. */
+typedef struct turner_tree_file turner_tree_file;
+/* 64-bit content key of a triangle set (the arrays turner_kdtree_build takes). */
+uint64_t turner_mesh_key(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris);
+/* Writes the tree under a temporary name and renames it to `path`. */
+int turner_kdtree_save(const turner_kdtree* tree, uint64_t key, const char* path);
+/* Reads a tree file; key != 0 must match the stored key. A bad magic, size,
+ * key or checksum is TURNER_ERR_BAD_SCENE. */
+int turner_kdtree_load(const char* path, uint64_t key, turner_kdtree** out);
+/* turner_kdtree_build through a cache directory: loads <dir>/<key>.tkd when
+ * it is valid for these triangles, else builds and writes it. cache_dir NULL
+ * builds without a cache. *from_cache (may be NULL) tells which happened. */
+int turner_kdtree_build_cached(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris,
+                               int threads, const char* cache_dir, turner_kdtree** out, int* from_cache);
+/* Maps a tree file read-only (no copy); the arrays can go straight to
+ * turner_upload_scene. verify != 0 checks the payload checksum. */
+int turner_tree_file_map(const char* path, uint64_t key, int verify, turner_tree_file** out);
+const uint64_t* turner_tree_file_nodes(const turner_tree_file* file, uint32_t* n_nodes);
+const turner_triangle* turner_tree_file_triangles(const turner_tree_file* file, uint32_t* n_tris);
+const float* turner_tree_file_box(const turner_tree_file* file);
+uint64_t turner_tree_file_key(const turner_tree_file* file);
+void turner_tree_file_unmap(turner_tree_file* file);
+
 /* ------------------------------------------------------------ scenes */
 /* Seeded synthetic scenes (the reference loads .blend files through assimp,
  * which this build does not ship):

@@ -144,3 +144,28 @@ def test_p3_of_gpu_image(ctx):
     p3 = tg.write_p3(img)
     assert p3 == orc.write_p3(img)
     assert p3.startswith("P3\n16 16\n255\n")
+
+
+def test_tree_file_upload_and_cli_cache(ctx, tmp_path):
+    """A mapped tree file uploads without a copy and renders the same image as
+    the freshly built tree; the CLI's --kdtree-cache builds once, then loads,
+    and writes the same P3 both times."""
+    import subprocess
+    m = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=3)
+    t = tg.KDTree.from_mesh(m)
+    key = tg.mesh_key(m.vertices, m.normals, m.diffuse)
+    t.save(tmp_path / "s.tkd", key)
+    f = tg.TreeFile(tmp_path / "s.tkd", key)
+    sid_file = ctx.upload(f.nodes, f.triangles, f.box)
+    sid_tree = ctx.upload_tree(t)
+    f.close()
+    a, _ = ctx.render([tg.make_job(sid_file, m, 40, 40, pixel_samples=2, max_depth=3, seed=5)])
+    b, _ = ctx.render([tg.make_job(sid_tree, m, 40, 40, pixel_samples=2, max_depth=3, seed=5)])
+    assert np.array_equal(a[0], b[0])
+    cli = tg.LIB_DIR / "turner_pathtracer"
+    cmd = [str(cli), "sphere:3", "-w", "32", "-p", "2", "-m", "1", "--kdtree-cache", str(tmp_path / "cache")]
+    r1 = subprocess.run(cmd, capture_output=True, text=True)
+    r2 = subprocess.run(cmd, capture_output=True, text=True)
+    assert r1.returncode == 0 and r2.returncode == 0, r1.stderr + r2.stderr
+    assert "Loaded kd-tree" not in r1.stderr and "Loaded kd-tree" in r2.stderr
+    assert r1.stdout == r2.stdout and r1.stdout.startswith("P3\n32 32\n255\n")

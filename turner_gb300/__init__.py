@@ -146,6 +146,17 @@ def _lib() -> C.CDLL:
         "turner_kdtree_export": (C.c_int, [_P, _P, _P, _P]),
         "turner_upload_kdtree": (C.c_int, [_P, _P, C.POINTER(C.c_uint32)]),
         "turner_kdtree_free": (None, [_P]),
+        "turner_mesh_key": (C.c_uint64, [_P, _P, _P, C.c_uint32]),
+        "turner_kdtree_save": (C.c_int, [_P, C.c_uint64, C.c_char_p]),
+        "turner_kdtree_load": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(_P)]),
+        "turner_kdtree_build_cached": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, C.c_char_p, C.POINTER(_P),
+                                                 C.POINTER(C.c_int)]),
+        "turner_tree_file_map": (C.c_int, [C.c_char_p, C.c_uint64, C.c_int, C.POINTER(_P)]),
+        "turner_tree_file_nodes": (_P, [_P, C.POINTER(C.c_uint32)]),
+        "turner_tree_file_triangles": (_P, [_P, C.POINTER(C.c_uint32)]),
+        "turner_tree_file_box": (_P, [_P]),
+        "turner_tree_file_key": (C.c_uint64, [_P]),
+        "turner_tree_file_unmap": (None, [_P]),
         "turner_scene_make": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.POINTER(_P)]),
         "turner_mesh_num_triangles": (C.c_uint32, [_P]),
         "turner_mesh_vertices": (C.POINTER(C.c_float), [_P]),
@@ -219,22 +230,53 @@ def make_rays(n: int, box, seed: int) -> tuple[np.ndarray, np.ndarray]:
     return o, d
 
 
+def _mesh_arrays(vertices, normals, diffuse):
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+    nr = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    d = None if diffuse is None else np.ascontiguousarray(diffuse, np.float32).reshape(-1, 4)
+    return v, nr, d
+
+
+def mesh_key(vertices: np.ndarray, normals: np.ndarray | None = None, diffuse: np.ndarray | None = None) -> int:
+    """64-bit content key of a triangle set (the key of its tree file)."""
+    v, nr, d = _mesh_arrays(vertices, normals, diffuse)
+    return _lib().turner_mesh_key(_ptr(v), None if nr is None else _ptr(nr), None if d is None else _ptr(d),
+                                  v.shape[0])
+
+
 class KDTree:
-    """KDTree::KDTree(Triangles) (lib/kdtree.cpp:474-490) on host threads."""
+    """KDTree::KDTree(Triangles) (lib/kdtree.cpp:474-490) on host threads.
+
+    cache_dir: build through a directory of content-keyed tree files (load
+    when one is valid for these triangles, else build and write it)."""
 
     def __init__(self, vertices: np.ndarray, normals: np.ndarray | None = None, diffuse: np.ndarray | None = None,
-                 threads: int = 0):
+                 threads: int = 0, cache_dir: str | None = None):
         lib = _lib()
-        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
-        nr = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
-        d = None if diffuse is None else np.ascontiguousarray(diffuse, np.float32).reshape(-1, 4)
+        v, nr, d = _mesh_arrays(vertices, normals, diffuse)
         self._h = _P()
-        _check(lib.turner_kdtree_build(_ptr(v), None if nr is None else _ptr(nr), None if d is None else _ptr(d),
-                                       v.shape[0], threads, C.byref(self._h)), "turner_kdtree_build")
+        hit = C.c_int(0)
+        _check(lib.turner_kdtree_build_cached(_ptr(v), None if nr is None else _ptr(nr),
+                                              None if d is None else _ptr(d), v.shape[0], threads,
+                                              None if cache_dir is None else str(cache_dir).encode(),
+                                              C.byref(self._h), C.byref(hit)), "turner_kdtree_build_cached")
+        self.from_cache = bool(hit.value)
 
     @classmethod
-    def from_mesh(cls, mesh: Mesh, threads: int = 0) -> "KDTree":
-        return cls(mesh.vertices, mesh.normals, mesh.diffuse, threads)
+    def from_mesh(cls, mesh: Mesh, threads: int = 0, cache_dir: str | None = None) -> "KDTree":
+        return cls(mesh.vertices, mesh.normals, mesh.diffuse, threads, cache_dir)
+
+    @classmethod
+    def load(cls, path, key: int = 0) -> "KDTree":
+        """Reads a tree file (key != 0 must match the stored one)."""
+        t = cls.__new__(cls)
+        t._h = _P()
+        _check(_lib().turner_kdtree_load(str(path).encode(), key, C.byref(t._h)), "turner_kdtree_load")
+        t.from_cache = True
+        return t
+
+    def save(self, path, key: int = 0) -> None:
+        _check(_lib().turner_kdtree_save(self._h, key, str(path).encode()), "turner_kdtree_save")
 
     def __del__(self):
         if getattr(self, "_h", None) and _LIB is not None:
@@ -257,6 +299,34 @@ class KDTree:
         box = np.empty(6, np.float32)
         _check(_lib().turner_kdtree_export(self._h, _ptr(nodes), _ptr(tris), _ptr(box)), "turner_kdtree_export")
         return nodes, tris, box
+
+
+class TreeFile:
+    """A tree file mapped read-only: nodes, triangles and box are zero-copy
+    views of the mapping, valid until close()."""
+
+    def __init__(self, path, key: int = 0, verify: bool = True):
+        lib = _lib()
+        self._h = _P()
+        _check(lib.turner_tree_file_map(str(path).encode(), key, 1 if verify else 0, C.byref(self._h)),
+               "turner_tree_file_map")
+        nn, nt = C.c_uint32(), C.c_uint32()
+        pn = lib.turner_tree_file_nodes(self._h, C.byref(nn))
+        pt = lib.turner_tree_file_triangles(self._h, C.byref(nt))
+        pb = lib.turner_tree_file_box(self._h)
+        self.key = lib.turner_tree_file_key(self._h)
+        self.nodes = np.ctypeslib.as_array(C.cast(pn, C.POINTER(C.c_uint64)), (nn.value,))
+        self.triangles = np.ctypeslib.as_array(C.cast(pt, C.POINTER(C.c_float)), (nt.value, TRIANGLE_FLOATS))
+        self.box = np.ctypeslib.as_array(C.cast(pb, C.POINTER(C.c_float)), (6,))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _LIB is not None:
+            self.nodes = self.triangles = self.box = None
+            _LIB.turner_tree_file_unmap(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def validate_nodes(nodes: np.ndarray, n_tris: int) -> tuple[int, int]:

@@ -39,6 +39,7 @@ HOST_UNITS = [
     CSRC / "host" / "scenes.cpp",
     CSRC / "host" / "kdtree_build.cpp",
     CSRC / "host" / "p3.cpp",
+    CSRC / "host" / "tree_file.cpp",
 ]
 
 

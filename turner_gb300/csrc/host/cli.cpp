@@ -40,6 +40,8 @@ GB300 options:
   --cosine                          Cosine-weighted bounces instead of uniform.
   --fast                            Early-exit closest-hit traversal for bounce rays.
   --device=<int>                    CUDA device [default: 0].
+  --kdtree-cache=<dir>              Directory of content-keyed kd-tree files: load the
+                                    scene's tree from it, or build and store it.
 
 Scenes: room | sphere[:DETAIL] | soup:COUNT[:SEED] | baffle[:DETAIL] | baffle-sphere[:DETAIL]
 )";
@@ -59,6 +61,7 @@ struct Options {
     uint64_t seed = 1;
     bool cosine = false, fast = false;
     int device = 0;
+    std::string kdtree_cache;
 };
 
 bool take(int& i, int argc, char** argv, const char* s, const char* l, std::string& val) {
@@ -115,6 +118,7 @@ int parse(int argc, char** argv, Options& o) {
         else if (a == "--cosine") o.cosine = true;
         else if (a == "--fast") o.fast = true;
         else if (take(i, argc, argv, nullptr, "--device", v)) o.device = std::stoi(v);
+        else if (take(i, argc, argv, nullptr, "--kdtree-cache", v)) o.kdtree_cache = v;
         else if (!a.empty() && a[0] != '-' && o.scene.empty()) o.scene = a;
         else return 2;
     }
@@ -166,12 +170,15 @@ int main(int argc, char** argv) {
     std::cerr << "Loading triangles and building kd-tree..." << std::endl;
     turner_kdtree* tree = nullptr;
     const auto t_tree = clock::now();
-    st = turner_kdtree_build(turner_mesh_vertices(mesh), turner_mesh_normals(mesh), turner_mesh_diffuse(mesh),
-                             turner_mesh_num_triangles(mesh), 0, &tree);
+    int from_cache = 0;
+    st = turner_kdtree_build_cached(turner_mesh_vertices(mesh), turner_mesh_normals(mesh), turner_mesh_diffuse(mesh),
+                                    turner_mesh_num_triangles(mesh), 0,
+                                    o.kdtree_cache.empty() ? nullptr : o.kdtree_cache.c_str(), &tree, &from_cache);
     if (st != TURNER_OK) {
         std::cerr << "kd-tree: " << turner_strerror(st) << std::endl;
         return 1;
     }
+    if (from_cache) std::cerr << "Loaded kd-tree from " << o.kdtree_cache << std::endl;
     const double tree_ms = std::chrono::duration<double, std::milli>(clock::now() - t_tree).count();
     std::cerr << "KDTree runtime: " << static_cast<long>(tree_ms) << std::endl;
     const double load_s = std::chrono::duration<double>(clock::now() - t_load).count();

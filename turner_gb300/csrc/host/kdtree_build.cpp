@@ -26,6 +26,7 @@
 // a size threshold are built on separate threads, and the tree is built
 // directly into an index-linked node pool.
 #include "turner_gpu.h"
+#include "tree.h"
 
 #include <algorithm>
 #include <cmath>
@@ -38,12 +39,6 @@
 #include <thread>
 #include <vector>
 
-struct turner_kdtree {
-    std::vector<uint64_t> nodes;
-    std::vector<turner_triangle> tris;
-    float box[6];
-    uint32_t height = 0;
-};
 
 namespace {
 
