@@ -112,8 +112,14 @@ typedef struct turner_job {
     uint32_t height;              /* the reference uses int(width / aspect)   */
     uint32_t pixel_samples;       /* -p                                       */
     int32_t max_depth;            /* -d: rays are traced at depths 0..max_depth */
-    int32_t monte_carlo_samples;  /* -m: 0 or 1 (the branching estimator of -m>1
-                                     is not implemented: TURNER_ERR_UNSUPPORTED) */
+    int32_t monte_carlo_samples;  /* -m: bounce rays per hit (0..TURNER_MAX_MC). With
+                                     M > 1 (pathtracer.cpp:72-88) child k of a hit
+                                     draws from its own stream, derived from its
+                                     parent's (a wavefront cannot follow the
+                                     reference's depth-first draws); a path has up
+                                     to M^max_depth rays at its widest level, and
+                                     passes shrink to fit them (at most 2^26 per
+                                     path: TURNER_ERR_TOO_LARGE). Not with GUIDED. */
     float exposure;               /* --exposure                               */
     float inverse_gamma;          /* --inverse-gamma                          */
     int32_t gamma_correction;     /* 0 for --no-gamma-correction              */
@@ -129,6 +135,9 @@ typedef struct turner_job {
                                      without exposure and gamma (for error
                                      measurements against converged images) */
 } turner_job;
+
+/* Largest -m. */
+#define TURNER_MAX_MC 64
 
 /* Jobs per turner_render call. */
 #define TURNER_MAX_JOBS 4096

@@ -94,6 +94,17 @@ inline uint64_t splitmix64(uint64_t x) {
     return z ^ (z >> 31);
 }
 
+// Branching estimator (-m > 1): child k of a hit draws from its own stream,
+// derived from the stream state of the ray that made the hit, so that every
+// ray of the tree has a stream that does not depend on traversal order (the
+// reference draws them depth-first from one thread-local generator,
+// lib/sampling.h:12, which a wavefront cannot reproduce). -m 1 keeps one
+// stream per path.
+inline uint64_t branch_seed(uint64_t parent_state, uint32_t k) {
+    const uint64_t s = splitmix64(parent_state ^ (0xA0761D6478BD642FULL * (uint64_t(k) + 1)));
+    return s ? s : 1;
+}
+
 // Harness seeding per (pixel, sample): key = pixel_index * spp + sample.
 inline void path_seeds(uint64_t seed, uint64_t key, uint64_t& jitter, uint64_t& bounce) {
     uint64_t a = splitmix64(seed ^ key);
@@ -352,9 +363,12 @@ C4 trace(const Ray& ray, Intersector& ti, const std::vector<Light>& lights, int 
     C4 indirect;
     float m[9];
     from_to_matrix(V3{0, 0, 1}, normal, m);
+    const uint64_t parent_state = uniform.s;
     for (int run = 0; run < conf.mc_samples; ++run) {
-        const float u1 = uniform.next_float();
-        const float u2 = uniform.next_float();
+        Xorshift branch{conf.mc_samples > 1 ? branch_seed(parent_state, static_cast<uint32_t>(run)) : 0};
+        Xorshift& gen = conf.mc_samples > 1 ? branch : uniform;
+        const float u1 = gen.next_float();
+        const float u2 = gen.next_float();
         float x, y, z, weight;
         if (conf.sampling == 0) {
             // sampling::hemisphere (lib/sampling.h:20-32): uniform, z = u1
@@ -374,7 +388,7 @@ C4 trace(const Ray& ray, Intersector& ti, const std::vector<Light>& lights, int 
             weight = 0.5f;
         }
         const V3 dir = mat_vec(m, V3{x, y, z});
-        const C4 li = trace(Ray{p2, dir}, ti, lights, depth + 1, conf, uniform, cnt);
+        const C4 li = trace(Ray{p2, dir}, ti, lights, depth + 1, conf, gen, cnt);
         indirect = indirect + weight * li;
     }
     if (conf.mc_samples > 0) {

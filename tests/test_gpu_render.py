@@ -61,6 +61,14 @@ CASES = {
     "soup_fast": (dict(kind=tg.SCENE_SOUP, count=5000, seed=2), dict(width=48, height=48, pixel_samples=2,
                                                                     max_depth=3, seed=4,
                                                                     traversal=tg.TRAVERSAL_FAST)),
+    # the branching estimator (-m > 1) under the per-branch stream contract
+    "room_mc2": (dict(kind=tg.SCENE_ROOM), dict(width=32, height=32, pixel_samples=2, max_depth=3,
+                                               monte_carlo_samples=2, seed=6)),
+    "sphere3_mc3_cosine": (dict(kind=tg.SCENE_SPHERE_ROOM, detail=3), dict(width=32, height=24, pixel_samples=2,
+                                                                          max_depth=2, monte_carlo_samples=3, seed=4,
+                                                                          sampling=tg.SAMPLING_COSINE)),
+    "room_mc8_default": (dict(kind=tg.SCENE_ROOM), dict(width=24, height=24, pixel_samples=1, max_depth=3,
+                                                       monte_carlo_samples=8, seed=2)),
 }
 
 
@@ -125,12 +133,42 @@ def test_render_is_deterministic(ctx):
     assert np.array_equal(a, b)
 
 
+def test_branching_passes_and_mixed_batches(ctx):
+    """-m > 1 jobs split into passes that hold every ray of their widest
+    level; radiance adds atomically there, so images agree to rounding. An
+    -m 1 job in the same batch stays bit-identical to its solo render."""
+    m, sid, _ = setup(ctx, kind=tg.SCENE_SPHERE_ROOM, detail=3)
+    branchy = tg.make_job(sid, m, 40, 30, pixel_samples=2, max_depth=3, monte_carlo_samples=4, seed=8)
+    plain = tg.make_job(sid, m, 24, 24, pixel_samples=4, max_depth=3, seed=9)
+    (a,), (sa,) = ctx.render([branchy])
+    ctx.set_chunk_paths(4096)
+    try:
+        (b,), (sb,) = ctx.render([branchy])
+    finally:
+        ctx.set_chunk_paths(1 << 24)
+    check_close(b, a, frac=1.0, tol=1e-5, mean_tol=1e-6)
+    assert sa.rays == sb.rays
+    (p_alone,), _ = ctx.render([plain])
+    (bb, pb), (sbb, spb) = ctx.render([branchy, plain])
+    assert np.array_equal(pb, p_alone)
+    check_close(bb, a, frac=1.0, tol=1e-5, mean_tol=1e-6)
+    assert sbb.rays == sa.rays
+
+
 def test_multi_light_and_mc_limits(ctx):
     m, sid, _ = setup(ctx, kind=tg.SCENE_ROOM)
-    job = tg.make_job(sid, m, 8, 8, monte_carlo_samples=2)
+    g = tg.Guide(ctx, seed=1)
+    ctx.set_guide(g)
+    job = tg.make_job(sid, m, 8, 8, monte_carlo_samples=2, sampling=tg.SAMPLING_GUIDED)
     with pytest.raises(tg.TurnerError) as e:
         ctx.render([job])
     assert e.value.status == tg.ERR_UNSUPPORTED
+    ctx.set_guide(None)
+    for mc, depth in ((65, 1), (64, 5)):
+        job = tg.make_job(sid, m, 8, 8, monte_carlo_samples=mc, max_depth=depth)
+        with pytest.raises(tg.TurnerError) as e:
+            ctx.render([job])
+        assert e.value.status == tg.ERR_TOO_LARGE
     job = tg.make_job(sid, m, 8, 8)
     job.n_lights = 2
     with pytest.raises(tg.TurnerError):

@@ -213,12 +213,26 @@ void fill_job(const turner_job& j, const SceneView& sc, JobDesc& d) {
     d.tone_map = 1;
 }
 
+// Rays of one path at its widest level: M^max_depth for the branching
+// estimator (-m M > 1), else 1; 0 if that exceeds 2^26.
+uint64_t branch_width(const turner_job& j) {
+    if (j.monte_carlo_samples <= 1) return 1;
+    uint64_t w = 1;
+    for (int d = 0; d < j.max_depth; ++d) {
+        w *= static_cast<uint64_t>(j.monte_carlo_samples);
+        if (w > (1ull << 26)) return 0;
+    }
+    return w;
+}
+
 int check_job(turner_ctx* ctx, const turner_job& j) {
     if (j.scene_id >= ctx->scenes.size() || !ctx->scenes[j.scene_id]->live) return TURNER_ERR_INVALID_ARG;
     if (j.width == 0 || j.height == 0 || j.pixel_samples == 0 || j.max_depth < 0) return TURNER_ERR_INVALID_ARG;
     if (!(j.camera.aspect > 0)) return TURNER_ERR_INVALID_ARG;
     if (j.monte_carlo_samples < 0 || j.n_lights < 0 || j.n_lights > 1) return TURNER_ERR_INVALID_ARG;
-    if (j.monte_carlo_samples > 1) return TURNER_ERR_UNSUPPORTED;
+    if (j.monte_carlo_samples > TURNER_MAX_MC) return TURNER_ERR_TOO_LARGE;
+    if (j.monte_carlo_samples > 1 && j.sampling == TURNER_SAMPLING_GUIDED) return TURNER_ERR_UNSUPPORTED;
+    if (branch_width(j) == 0) return TURNER_ERR_TOO_LARGE;
     if (j.sampling != TURNER_SAMPLING_UNIFORM && j.sampling != TURNER_SAMPLING_COSINE &&
         j.sampling != TURNER_SAMPLING_GUIDED)
         return TURNER_ERR_INVALID_ARG;
@@ -461,19 +475,20 @@ struct Batch {
     std::vector<JobDesc> table;
     std::vector<Chunk> chunks;
     uint64_t total_pixels = 0;
-    uint32_t cap = 0;                // paths per pass
+    uint32_t cap = 0;                // queue entries per pass (paths, or rays of a level with -m > 1)
     int levels = 0;                  // largest max_depth + 1
     bool single_scene = true;
     SceneView single{};
     uint32_t max_height = 0;         // deepest traversal stack any scene needs
     bool guided = false;             // some job samples with the learned proposal
+    bool branching = false;          // some job has -m > 1 (radiance is added atomically)
 };
 
 int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4* const* outs, bool tone_map,
                Batch& b) {
     b.table.resize(n_jobs);
-    uint64_t pixels = 0, paths = 0;
-    uint32_t max_spp = 1;
+    uint64_t pixels = 0, paths = 0, load = 0, max_load = 1;
+    std::vector<uint64_t> width(n_jobs);
     for (uint32_t j = 0; j < n_jobs; ++j) {
         fill_job(jobs[j], ctx->scenes[jobs[j].scene_id]->view, b.table[j]);
         JobDesc& d = b.table[j];
@@ -483,7 +498,10 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
         d.out = outs ? outs[j] : nullptr;
         pixels += uint64_t(d.width) * d.height;
         paths += uint64_t(d.width) * d.height * d.spp;
-        max_spp = std::max(max_spp, d.spp);
+        width[j] = branch_width(jobs[j]);
+        load += uint64_t(d.width) * d.height * d.spp * width[j];
+        max_load = std::max<uint64_t>(max_load, uint64_t(d.spp) * width[j]);
+        if (width[j] > 1) b.branching = true;
         b.levels = std::max(b.levels, d.max_depth + 1);
         if (jobs[j].scene_id != jobs[0].scene_id) b.single_scene = false;
         b.max_height = std::max(b.max_height, d.sc.height);
@@ -491,22 +509,27 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
     }
     b.total_pixels = pixels;
     b.single = b.table[0].sc;
-    b.cap = static_cast<uint32_t>(std::min<uint64_t>(paths, std::max<uint64_t>(ctx->chunk_paths, max_spp)));
-    // whole pixels, at most cap paths per chunk; a chunk may span several jobs
-    Chunk c{0, 0, 0, 0};
+    if (max_load > (1ull << 30)) return TURNER_ERR_TOO_LARGE;   // one pixel must fit a pass
+    b.cap = static_cast<uint32_t>(std::min<uint64_t>(load, std::max<uint64_t>(ctx->chunk_paths, max_load)));
+    (void)paths;
+    // whole pixels, at most cap queue entries per level per chunk; a chunk
+    // may span several jobs
+    Chunk c{0, 0, 0, 0, 0};
     for (uint32_t j = 0; j < n_jobs; ++j) {
         const JobDesc& d = b.table[j];
+        const uint64_t per_pixel = uint64_t(d.spp) * width[j];
         uint64_t left = uint64_t(d.width) * d.height;
         while (left > 0) {
-            const uint64_t room = (b.cap - c.n_paths) / d.spp;
+            const uint64_t room = (b.cap - c.n_rays) / per_pixel;
             if (room == 0) {
                 b.chunks.push_back(c);
-                c = Chunk{c.pixel0 + c.n_pixels, c.path0 + c.n_paths, 0, 0};
+                c = Chunk{c.pixel0 + c.n_pixels, c.path0 + c.n_paths, 0, 0, 0};
                 continue;
             }
             const uint64_t take = std::min(room, left);
             c.n_pixels += static_cast<uint32_t>(take);
             c.n_paths += static_cast<uint32_t>(take * d.spp);
+            c.n_rays += static_cast<uint32_t>(take * per_pixel);
             left -= take;
         }
     }
@@ -602,7 +625,7 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             shadow_cfg.work = cnt + 3 * (b.levels + 1) + depth;
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
-                launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_paths, fast, trace_cfg, ctx->stream);
+                launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_rays, fast, trace_cfg, ctx->stream);
             }
             if (b.guided && depth + 1 < b.levels) {
                 {
@@ -619,11 +642,12 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
                 launch_shade(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts, gq,
-                             recs, c.n_paths, ctx->stream);
+                             recs, c.n_rays, ctx->stream);
             }
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
-                launch_shadow(single, jobs, sh, ctx->L.as<float4>(), c.n_paths, shadow_cfg, ctx->stream);
+                launch_shadow(single, jobs, sh, ctx->L.as<float4>(), c.n_rays, b.branching, shadow_cfg,
+                              ctx->stream);
             }
             std::swap(cur, nxt);
         }

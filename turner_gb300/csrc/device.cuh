@@ -346,6 +346,13 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 }
 
 // Per-(pixel, sample) streams: key = pixel_index * spp + sample.
+// Stream of child k of a hit under the branching estimator (-m > 1), derived
+// from the stream state of the ray that made the hit (same as the oracle's).
+__device__ __forceinline__ uint64_t branch_seed(uint64_t parent_state, uint32_t k) {
+    const uint64_t s = splitmix64(parent_state ^ (0xA0761D6478BD642FULL * (uint64_t(k) + 1)));
+    return s ? s : 1;
+}
+
 __device__ __forceinline__ void path_seeds(uint64_t seed, uint64_t key, uint64_t& jitter, uint64_t& bounce) {
     const uint64_t a = splitmix64(seed ^ key);
     const uint64_t b = splitmix64(a ^ 0xD1B54A32D192ED03ULL);

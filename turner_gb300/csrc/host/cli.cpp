@@ -33,7 +33,7 @@ Options:
 Pathtracer options:
   -d --max-depth=<int>              Maximum recursion depth for raytracing [default: 3].
   -p --pixel-samples=<int>          Number of samples per pixel [default: 1].
-  -m --monte-carlo-samples=<int>    Monte Carlo samples per ray (0 or 1) [default: 8].
+  -m --monte-carlo-samples=<int>    Monte Carlo samples per ray [default: 8].
 
 GB300 options:
   --seed=<int>                      Stream seed base [default: 1].
@@ -205,8 +205,7 @@ int main(int argc, char** argv) {
     job.height = static_cast<uint32_t>(static_cast<int>(o.width / cam.aspect));   // main.cpp:179
     job.pixel_samples = static_cast<uint32_t>(o.pixel_samples);
     job.max_depth = o.depth;
-    job.monte_carlo_samples = o.mc > 1 ? 1 : o.mc;
-    if (o.mc > 1) std::cerr << "note: -m " << o.mc << " is traced as -m 1 (one bounce sample per hit)" << std::endl;
+    job.monte_carlo_samples = o.mc;
     job.exposure = o.exposure;
     job.inverse_gamma = o.inverse_gamma;
     job.gamma_correction = o.gamma ? 1 : 0;

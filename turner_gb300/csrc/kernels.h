@@ -73,10 +73,13 @@ struct JobDesc {
 };
 
 // A render pass: whole pixels [pixel0, pixel0 + n_pixels) of the batch's
-// pixel space, which are paths [path0, path0 + n_paths).
+// pixel space, which are paths [path0, path0 + n_paths). With -m = M > 1 a
+// path has up to M^max_depth rays at its widest level, so the queues hold
+// n_rays entries.
 struct Chunk {
     uint64_t pixel0, path0;
     uint32_t n_pixels, n_paths;
+    uint32_t n_rays;   // bound on the rays of one level (n_paths unless -m > 1 branches)
 };
 
 // How traversal kernels are launched. persistent: one grid of resident
@@ -112,8 +115,10 @@ void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit*
 // Network inputs for the hits of guided jobs that will bounce (zeros elsewhere).
 void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, const Hit* hits, float* feat,
                            uint32_t capacity, cudaStream_t stream);
+// atomic_l: add to L atomically (batches with -m > 1, where several shadow
+// rays of one path are in the queue at once).
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
-                   const TraverseCfg& cfg, cudaStream_t stream);
+                   bool atomic_l, const TraverseCfg& cfg, cudaStream_t stream);
 void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream);
 // acc[p] += (double) sum of the chunk's sample radiance for pixel p (linear)
 void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, double4* acc,

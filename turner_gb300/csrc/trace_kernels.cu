@@ -44,6 +44,31 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
     return base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
 }
 
+// Appends `cnt` entries per lane (one atomic per warp); returns this lane's
+// first slot. Every lane of the warp must call it.
+__device__ __forceinline__ uint32_t warp_append_n(uint32_t* counter, uint32_t cnt) {
+    const uint32_t lane = lane_id();
+    uint32_t x = cnt;   // inclusive prefix sum over the warp
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if (lane >= static_cast<uint32_t>(off)) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, x, 31);
+    if (total == 0) return 0;
+    uint32_t base = 0;
+    if (lane == 31) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    return base + x - cnt;
+}
+
+__device__ __forceinline__ void atomic_add4(float4* p, float4 v) {
+    atomicAdd(&p->x, v.x);
+    atomicAdd(&p->y, v.y);
+    atomicAdd(&p->z, v.z);
+    atomicAdd(&p->w, v.w);
+}
+
 // Job owning global path g / global pixel p (job offsets ascend).
 __device__ __forceinline__ uint32_t job_of_path(const JobDesc* jobs, uint32_t n_jobs, uint64_t g) {
     uint32_t lo = 0, hi = n_jobs;
@@ -179,6 +204,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
         bool emit_shadow = false, emit_bounce = false;
         float4 sh_o, sh_d, sh_c, b_o, b_d, b_T;
         uint2 b_rng;
+        // -m > 1: n_branch children, each on its own stream derived from br_state
+        uint32_t n_branch = 0, br_path = 0;
+        uint64_t br_state = 0;
+        float3 br_nrm = make_float3(0.f, 0.f, 0.f), br_p2 = br_nrm;
+        float4 br_Td = make_float4(0.f, 0.f, 0.f, 0.f);
         uint32_t jidx = 0;
         bool emit_record = false;
         float rec_dir[3] = {0.f, 0.f, 0.f}, rec_t = 0.f, rec_fcp = 0.f;
@@ -197,8 +227,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                 if (r != kNoRecord) recs.l_before[r] = luminance(L[path]);
             }
             if (h.id >= kMiss) {
-                // miss: trace() returns conf.bg_color (alpha 1)
-                L[path] = add4(L[path], mul4(T, make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f)));
+                // miss: trace() returns conf.bg_color (alpha 1); with -m > 1 several rays
+                // of one path are live at a time, so they add atomically
+                const float4 add = mul4(T, make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f));
+                if (job.mc > 1) atomic_add4(L + path, add);
+                else L[path] = add4(L[path], add);
             } else {
                 const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
                 const float4* rec = job.sc.shade + 4 * size_t(h.id);
@@ -224,7 +257,15 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                         emit_shadow = true;
                     }
                 }
-                if (depth < job.max_depth && job.mc > 0) {
+                if (depth < job.max_depth && job.mc > 1) {
+                    const uint2 r2 = in.rng[i];
+                    n_branch = static_cast<uint32_t>(job.mc);
+                    br_state = uint64_t(r2.x) | (uint64_t(r2.y) << 32);
+                    br_nrm = nrm;
+                    br_p2 = p2;
+                    br_Td = Td;
+                    br_path = path;
+                } else if (depth < job.max_depth && job.mc > 0) {
                     float m[9];
                     from_to_z(nrm, m);
                     const uint2 r2 = in.rng[i];
@@ -347,6 +388,43 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
             out.rng[bi] = b_rng;
             if (out.rec) out.rec[bi] = b_rec;
         }
+        // the branching estimator (pathtracer.cpp:72-88 with M > 1): indirect is
+        // the mean over M children, so each carries 1/M of the weight
+        const uint32_t bb = warp_append_n(out.count, n_branch);
+        if (n_branch) {
+            const JobDesc& job = jobs[jidx];
+            float m[9];
+            from_to_z(br_nrm, m);
+            const float inv_m = 1.f / static_cast<float>(n_branch);
+            for (uint32_t k = 0; k < n_branch; ++k) {
+                uint64_t cs = branch_seed(br_state, k);
+                const float u1 = xorshift_float(cs);
+                const float u2 = xorshift_float(cs);
+                float x, y, z, weight;
+                if (job.sampling == 0) {
+                    z = u1;
+                    const float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+                    const float phi = 6.28318548202514648438f * u2;
+                    x = rr * cosf(phi);
+                    y = rr * sinf(phi);
+                    weight = 2.f * u1;
+                } else {
+                    const float rr = sqrtf(u1);
+                    z = sqrtf(fmaxf(0.f, 1.f - u1));
+                    const float phi = 6.28318548202514648438f * u2;
+                    x = rr * cosf(phi);
+                    y = rr * sinf(phi);
+                    weight = 1.f;
+                }
+                const uint32_t slot = bb + k;
+                out.o[slot] = make_float4(br_p2.x, br_p2.y, br_p2.z, __uint_as_float(br_path));
+                out.d[slot] = make_float4(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
+                                          m[6] * x + m[7] * y + m[8] * z, __uint_as_float(jidx));
+                out.T[slot] = scale4(weight * inv_m, br_Td);
+                out.rng[slot] = make_uint2(static_cast<uint32_t>(cs), static_cast<uint32_t>(cs >> 32));
+                if (out.rec) out.rec[slot] = kNoRecord;
+            }
+        }
     }
 }
 
@@ -376,6 +454,7 @@ struct ShadowSrc {          // any hit of a shadow queue -> direct light if unbl
     const uint32_t* jobs;
     const uint32_t* cnt;
     float4* L;
+    bool atomic_l;          // -m > 1 in the batch: several shadow rays of one path per level
     __device__ uint32_t count() const { return *cnt; }
     __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax, uint32_t& job) const {
         const float4 a = o[i], b = d[i];
@@ -388,8 +467,12 @@ struct ShadowSrc {          // any hit of a shadow queue -> direct light if unbl
         if (h.id >= kMiss) {
             const uint32_t path = __float_as_uint(o[i].w);
             const float4 ci = c[i];
-            float4 l = L[path];
-            L[path] = make_float4(l.x + ci.x, l.y + ci.y, l.z + ci.z, l.w + ci.w);
+            if (atomic_l) {
+                atomic_add4(L + path, ci);
+            } else {
+                const float4 l = L[path];
+                L[path] = make_float4(l.x + ci.x, l.y + ci.y, l.z + ci.z, l.w + ci.w);
+            }
         }
     }
 };
@@ -616,7 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_flat(SceneView single, const J
 }
 
 __global__ void __launch_bounds__(kBlock) k_shadow_flat(SceneView single, const JobDesc* __restrict__ jobs, bool multi,
-                                                        ShadowQueue sh, float4* __restrict__ L) {
+                                                        ShadowQueue sh, float4* __restrict__ L, bool atomic_l) {
     const uint32_t n = *sh.count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 o = sh.o[i];
@@ -625,7 +708,8 @@ __global__ void __launch_bounds__(kBlock) k_shadow_flat(SceneView single, const 
         const Hit h = traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w);
         if (h.id >= kMiss) {
             const uint32_t path = __float_as_uint(o.w);
-            L[path] = add4(L[path], sh.c[i]);
+            if (atomic_l) atomic_add4(L + path, sh.c[i]);
+            else L[path] = add4(L[path], sh.c[i]);
         }
     }
 }
@@ -680,15 +764,15 @@ void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, co
 }
 
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
-                   const TraverseCfg& cfg, cudaStream_t stream) {
+                   bool atomic_l, const TraverseCfg& cfg, cudaStream_t stream) {
     const SceneView sv = single ? *single : SceneView{};
     if (cfg.persistent) {
-        const ShadowSrc src{sh.o, sh.d, sh.c, sh.job, sh.count, L};
+        const ShadowSrc src{sh.o, sh.d, sh.c, sh.job, sh.count, L, atomic_l};
         if (single) run_traverse<ShadowSrc, true, false, false>(sv, jobs, src, capacity, cfg, stream);
         else run_traverse<ShadowSrc, true, false, true>(sv, jobs, src, capacity, cfg, stream);
         return;
     }
-    k_shadow_flat<<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, sh, L);
+    k_shadow_flat<<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, sh, L, atomic_l);
 }
 
 void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream) {
