@@ -363,6 +363,10 @@ uint32_t turner_kdtree_height(const turner_kdtree* tree);
 int turner_kdtree_export(const turner_kdtree* tree, uint64_t* nodes, turner_triangle* tris, float box[6]);
 int turner_upload_kdtree(turner_ctx* ctx, const turner_kdtree* tree, uint32_t* scene_id);
 void turner_kdtree_free(turner_kdtree* tree);
+/* Sets the reflective colour and reflectivity of every triangle record
+ * (n_tris * 5 floats: r, g, b, a, reflectivity), the material fields the
+ * Whitted raytracer reads (raytracer.cpp:46-55). They do not change the tree. */
+int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective);
 
 /* ---------------------------------------------------------- tree files */
 /* A binary file holding one kd-tree (node words, triangle records, box),
@@ -403,18 +407,24 @@ void turner_tree_file_unmap(turner_tree_file* file);
  *   2 SOUP         clustered triangle soup of `count` triangles in the room
  *   3 BAFFLE_ROOM  walls tessellated detail x detail quads, a 1.5x1.5 baffle
  *                  0.3 below the light
- *   4 BAFFLE_SPHERE the SPHERE_ROOM sphere inside the BAFFLE_ROOM room */
+ *   4 BAFFLE_SPHERE the SPHERE_ROOM sphere inside the BAFFLE_ROOM room
+ *   5 MIRROR_ROOM  the ROOM with reflective boxes (reflectivity 0.3 and 0.85),
+ *                  for the raytracer */
 #define TURNER_SCENE_ROOM 0
 #define TURNER_SCENE_SPHERE_ROOM 1
 #define TURNER_SCENE_SOUP 2
 #define TURNER_SCENE_BAFFLE_ROOM 3
 #define TURNER_SCENE_BAFFLE_SPHERE 4
+#define TURNER_SCENE_MIRROR_ROOM 5
 
 int turner_scene_make(int kind, uint32_t detail, uint32_t count, uint64_t seed, float aspect, turner_mesh** out);
 uint32_t turner_mesh_num_triangles(const turner_mesh* mesh);
 const float* turner_mesh_vertices(const turner_mesh* mesh); /* n*9 */
 const float* turner_mesh_normals(const turner_mesh* mesh);  /* n*9 */
 const float* turner_mesh_diffuse(const turner_mesh* mesh);  /* n*4 */
+/* n*5: reflective colour (rgba) and reflectivity per triangle (zeros where a
+ * scene has no mirrors); give it to turner_kdtree_set_reflective. */
+const float* turner_mesh_reflective(const turner_mesh* mesh);
 /* Camera as the scene defines it; *hfov receives aiCamera::mHorizontalFOV. */
 void turner_mesh_camera(const turner_mesh* mesh, turner_camera* cam, float* hfov);
 /* Returns the number of lights (0 or 1) and copies the first. */

@@ -22,6 +22,14 @@ g++ "${FLAGS[@]}" -c "$REF/lib/kdtree.cpp" -o "$OUT/kdtree.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/geometry_prelude.cpp" -o "$OUT/geometry_prelude.o" & pids+=($!)
 g++ "${FLAGS[@]}" -c "$HERE/ref_fixtures.cpp" -o "$OUT/ref_fixtures.o" & pids+=($!)
+# the raytracer and raycaster each define trace() and USAGE: one translation
+# unit each, with those names (and the raytracer's copy of the header-defined
+# lambertian()) renamed
+g++ "${FLAGS[@]}" -Dtrace=ref_raytracer_trace -DUSAGE=ref_raytracer_USAGE -Dlambertian=ref_raytracer_lambertian -c "$REF/raytracer.cpp" \
+    -o "$OUT/raytracer.o" & pids+=($!)
+g++ "${FLAGS[@]}" -Dtrace=ref_raycaster_trace -DUSAGE=ref_raycaster_USAGE -c "$REF/raycaster.cpp" \
+    -o "$OUT/raycaster.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
-g++ -shared -o "$OUT/libturner_ref.so" "$OUT/kdtree.o" "$OUT/ref_driver.o" "$OUT/geometry_prelude.o" "$OUT/ref_fixtures.o" -lpthread
+g++ -shared -o "$OUT/libturner_ref.so" "$OUT/kdtree.o" "$OUT/ref_driver.o" "$OUT/geometry_prelude.o" \
+    "$OUT/ref_fixtures.o" "$OUT/raytracer.o" "$OUT/raycaster.o" -lpthread
 echo "build_ref: wrote $OUT/libturner_ref.so"

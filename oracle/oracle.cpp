@@ -322,6 +322,9 @@ struct Conf {
     int mc_samples = 1;
     int sampling = 0;   // 0 = uniform hemisphere (reference), 1 = cosine-weighted
     C4 bg{0, 0, 0, 1};
+    int renderer = 0;   // 0 path tracer, 1 Whitted raytracer, 2 raycaster
+    float shadow_intensity = 0.5f;
+    float max_visibility = 2.f;
 };
 
 struct Counters {
@@ -400,6 +403,64 @@ C4 trace(const Ray& ray, Intersector& ti, const std::vector<Light>& lights, int 
     return diffuse * (direct * static_cast<float>(M_1_PI) + indirect * 2.f);
 }
 
+// trace() of the Whitted raytracer (raytracer.cpp:5-67): Lambertian direct
+// light (lib/lambertian.h:15-19), a mirror bounce when the triangle is
+// reflective, and a shadow test that darkens the whole colour by
+// shadow_intensity. Every call counts as a ray, also the one past max depth.
+C4 trace_whitted(const Ray& ray, Intersector& ti, const Light& light, int depth, const Conf& conf, Counters& cnt) {
+    cnt.rays += 1;
+    if (depth > conf.max_depth) return C4{};
+
+    float dist_to_triangle = 0, s = 0, t = 0;
+    const uint32_t id = ti.intersect(ray, dist_to_triangle, s, t);
+    if (id >= kMaxTriangleId) return conf.bg;
+
+    const V3 p = ray.o + dist_to_triangle * ray.d;
+    V3 light_dir = normalize(light.position - p);
+    const Tri& tri = ti.sc->tris[id];
+    const float w0 = 1.f - s - t;
+    const V3 normal = normalize(w0 * tri.normals[0] + s * tri.normals[1] + t * tri.normals[2]);
+    const C4 diffuse{tri.diffuse[0], tri.diffuse[1], tri.diffuse[2], tri.diffuse[3]};
+    const float cos_alpha = std::max(0.f, dot(light_dir, normal));
+    const C4 direct = cos_alpha * diffuse * light.color;
+    const V3 p2 = p + normal * 0.0001f;
+
+    C4 color = direct;
+    if (tri.reflectivity > 0) {
+        // reflected direction d - 2 (n.d) n
+        const V3 refl = ray.d - (2.f * dot(normal, ray.d)) * normal;
+        const C4 reflected = trace_whitted(Ray{p2, refl}, ti, light, depth + 1, conf, cnt);
+        const C4 rc{tri.reflective[0], tri.reflective[1], tri.reflective[2], tri.reflective[3]};
+        color = (1.f - tri.reflectivity) * direct + tri.reflectivity * rc * reflected;
+    }
+
+    light_dir = normalize(light.position - p2);
+    const float dist_to_light = length(light.position - p2);
+    float dist_to_next = 0;
+    cnt.shadow_rays += 1;
+    const uint32_t sh = ti.intersect(Ray{p2, light_dir}, dist_to_next, s, t);
+    if (sh < kMaxTriangleId && dist_to_next < dist_to_light) {
+        const C4 dark = color * conf.shadow_intensity;
+        color = C4{color.r - dark.r, color.g - dark.g, color.b - dark.b, color.a - dark.a};
+    }
+    return color;
+}
+
+// trace() of the raycaster (raycaster.cpp:6-24): the diffuse colour, its alpha
+// replaced by the fall-off 1 - r / max_visibility clamped to [0, 1]; only
+// hits count as rays.
+C4 trace_cast(const Ray& ray, Intersector& ti, const Conf& conf, Counters& cnt) {
+    float dist_to_triangle = 0, s = 0, t = 0;
+    const uint32_t id = ti.intersect(ray, dist_to_triangle, s, t);
+    if (id >= kMaxTriangleId) return conf.bg;
+    cnt.rays += 1;
+    const Tri& tri = ti.sc->tris[id];
+    C4 res{tri.diffuse[0], tri.diffuse[1], tri.diffuse[2], tri.diffuse[3]};
+    const float a = 1.f - (dist_to_triangle / conf.max_visibility);
+    res.a = a < 0.f ? 0.f : (a > 1.f ? 1.f : a);
+    return res;
+}
+
 // lib/effects.h:15-49
 inline float exposure(float light, float value) { return 1 - expf(-light * value); }
 inline float gamma_fn(float light, float inverse_gamma) { return powf(light, inverse_gamma); }
@@ -430,6 +491,9 @@ struct orc_params {
     float light_color[4];
     int32_t sampling;       // 0 uniform (reference), 1 cosine
     int32_t tone_map;       // 1: divide, exposure, gamma (main.cpp:216-223); 0: mean only
+    int32_t renderer;       // 0 path tracer, 1 raytracer, 2 raycaster
+    float shadow_intensity; // raytracer --shadow
+    float max_visibility;   // raycaster --max-visibility
 };
 
 void* orc_scene_create(const uint64_t* nodes, uint64_t n_nodes, const float* tri48, uint64_t n_tris,
@@ -499,6 +563,9 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
     conf.mc_samples = p->monte_carlo_samples;
     conf.sampling = p->sampling;
     conf.bg = C4{p->background[0], p->background[1], p->background[2], 1};
+    conf.renderer = p->renderer;
+    conf.shadow_intensity = p->shadow_intensity;
+    conf.max_visibility = p->max_visibility;
     std::vector<Light> lights;
     if (p->n_lights > 0) {
         lights.push_back(Light{V3{p->light_position[0], p->light_position[1], p->light_position[2]},
@@ -534,7 +601,9 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
                     const V3 v{-dx_cam * (1 - 2 * px / w), dy_cam * (1 - 2 * py / h), -1};
                     const V3 d = mat_vec(cam->trafo, v);
                     ++prim;
-                    acc = acc + trace(Ray{cam_pos, d}, ti, lights, 0, conf, bnc, cnt);
+                    if (conf.renderer == 1) acc = acc + trace_whitted(Ray{cam_pos, d}, ti, lights.front(), 0, conf, cnt);
+                    else if (conf.renderer == 2) acc = acc + trace_cast(Ray{cam_pos, d}, ti, conf, cnt);
+                    else acc = acc + trace(Ray{cam_pos, d}, ti, lights, 0, conf, bnc, cnt);
                 }
                 float* o = out_rgba + 4 * (size_t(y) * width + x);
                 const float fs = static_cast<float>(spp);

@@ -30,7 +30,8 @@ class OrcParams(C.Structure):
                 ("max_depth", C.c_int32), ("monte_carlo_samples", C.c_int32), ("exposure", C.c_float),
                 ("inverse_gamma", C.c_float), ("gamma_correction", C.c_int32), ("background", C.c_float * 3),
                 ("seed", C.c_uint64), ("n_lights", C.c_int32), ("light_position", C.c_float * 3),
-                ("light_color", C.c_float * 4), ("sampling", C.c_int32), ("tone_map", C.c_int32)]
+                ("light_color", C.c_float * 4), ("sampling", C.c_int32), ("tone_map", C.c_int32),
+                ("renderer", C.c_int32), ("shadow_intensity", C.c_float), ("max_visibility", C.c_float)]
 
 
 class RefCamera(C.Structure):
@@ -43,7 +44,8 @@ class RefParams(C.Structure):
                 ("max_depth", C.c_int32), ("monte_carlo_samples", C.c_int32), ("exposure", C.c_float),
                 ("inverse_gamma", C.c_float), ("gamma_correction", C.c_int32), ("background", C.c_float * 3),
                 ("seed", C.c_uint64), ("n_lights", C.c_int32), ("light_position", C.c_float * 3),
-                ("light_color", C.c_float * 4), ("threads", C.c_int32)]
+                ("light_color", C.c_float * 4), ("threads", C.c_int32), ("renderer", C.c_int32),
+                ("shadow_intensity", C.c_float), ("max_visibility", C.c_float)]
 
 
 _ORC = None
@@ -90,7 +92,7 @@ def ref_lib() -> C.CDLL:
     if _REF is None:
         L = C.CDLL(str(REF_SO))
         L.ref_tree_build.restype = _P
-        L.ref_tree_build.argtypes = [_P, _P, _P, C.c_uint32]
+        L.ref_tree_build.argtypes = [_P, _P, _P, C.c_uint32, _P]
         L.ref_tree_free.argtypes = [_P]
         for f in ("ref_tree_num_nodes", "ref_tree_height", "ref_tree_num_triangles"):
             getattr(L, f).restype = C.c_uint64
@@ -141,9 +143,11 @@ class Scene:
     def render(self, camera, light, width: int, height: int, spp: int, max_depth: int, mc: int = 1,
                seed: int = 1, exposure: float = 1.0, inverse_gamma: float = 0.454545, gamma: bool = True,
                background=(0.0, 0.0, 0.0), sampling: int = 0, tone_map: bool = True, threads: int = 0,
-               rows: tuple[int, int] | None = None):
+               rows: tuple[int, int] | None = None, renderer: int = 0, shadow_intensity: float = 0.5,
+               max_visibility: float = 2.0):
         """Returns (image (h, w, 4) float32, stats [rays, primary, shadow, closest-hit node visits,
-        closest-hit triangle tests, shadow node visits, shadow triangle tests])."""
+        closest-hit triangle tests, shadow node visits, shadow triangle tests]).
+        renderer: 0 path tracer, 1 Whitted raytracer, 2 raycaster."""
         cam = OrcCamera()
         cam.position[:] = list(camera.position)
         cam.trafo[:] = list(camera.trafo)
@@ -163,6 +167,9 @@ class Scene:
             p.light_color[:] = list(light.color)
         p.sampling = sampling
         p.tone_map = 1 if tone_map else 0
+        p.renderer = renderer
+        p.shadow_intensity = shadow_intensity
+        p.max_visibility = max_visibility
         img = np.zeros((height, width, 4), np.float32)
         stats = np.zeros(7, np.uint64)
         r0, r1 = rows if rows else (0, 0)
@@ -212,13 +219,14 @@ def tone(rgba: np.ndarray, exposure: float, inverse_gamma: float, gamma: bool = 
 class RefTree:
     """The reference's KDTree built by oracle/_ref (checker only)."""
 
-    def __init__(self, vertices: np.ndarray, normals=None, diffuse=None):
+    def __init__(self, vertices: np.ndarray, normals=None, diffuse=None, reflective=None):
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
         self.n = v.shape[0]
         nr = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
         d = None if diffuse is None else np.ascontiguousarray(diffuse, np.float32).reshape(-1, 4)
-        self._keep = (v, nr, d)
-        self._h = ref_lib().ref_tree_build(_ptr(v), _ptr(nr), _ptr(d), self.n)
+        rf = None if reflective is None else np.ascontiguousarray(reflective, np.float32).reshape(-1, 5)
+        self._keep = (v, nr, d, rf)
+        self._h = ref_lib().ref_tree_build(_ptr(v), _ptr(nr), _ptr(d), self.n, _ptr(rf))
 
     def __del__(self):
         if getattr(self, "_h", None) and _REF is not None:
@@ -249,7 +257,9 @@ class RefTree:
         return hid, r, s, t
 
     def render(self, position, trafo, hfov, aspect, light, width, height, spp, max_depth, mc=1, seed=1,
-               exposure=1.0, inverse_gamma=0.454545, gamma=True, background=(0.0, 0.0, 0.0), threads=0):
+               exposure=1.0, inverse_gamma=0.454545, gamma=True, background=(0.0, 0.0, 0.0), threads=0,
+               renderer=0, shadow_intensity=0.5, max_visibility=2.0):
+        """renderer: 0 pathtracer.cpp, 1 raytracer.cpp, 2 raycaster.cpp."""
         cam = RefCamera()
         cam.position[:] = list(position)
         cam.trafo[:] = list(trafo)
@@ -268,6 +278,9 @@ class RefTree:
             p.light_position[:] = list(light.position)
             p.light_color[:] = list(light.color)
         p.threads = threads or os.cpu_count()
+        p.renderer = renderer
+        p.shadow_intensity = shadow_intensity
+        p.max_visibility = max_visibility
         img = np.zeros((height, width, 4), np.float32)
         stats = np.zeros(2, np.uint64)
         ref_lib().ref_render(self._h, C.byref(cam), C.byref(p), _ptr(img), _ptr(stats))

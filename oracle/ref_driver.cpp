@@ -6,6 +6,10 @@
 // What it wraps, unmodified:
 //   KDTree / KDTreeIntersection      lib/kdtree.h:187-308, lib/kdtree.cpp:474-607
 //   trace() (path tracer)            pathtracer.cpp:14-102 (included below)
+//   trace() (Whitted raytracer)      raytracer.cpp:5-67, compiled as ref_raytracer_trace
+//   trace() (raycaster)              raycaster.cpp:6-24, compiled as ref_raycaster_trace
+//                                    (oracle/build_ref.sh renames the symbol per
+//                                    translation unit: each renderer defines trace())
 //   Camera::raster2cam               lib/types.h:92-123
 //   exposure / gamma                 lib/effects.h:15-49
 // The render driver re-creates main.cpp:181-236 (row tasks, pixel loop,
@@ -15,6 +19,13 @@
 // that the image does not depend on thread scheduling.
 
 #include "pathtracer.cpp"
+
+// The raytracer's and the raycaster's trace() (trace.h:23-25), each from its
+// own translation unit with the symbol renamed (oracle/build_ref.sh).
+Color ref_raytracer_trace(const Ray& ray, KDTreeIntersection& tree_intersection, const std::vector<Light>& lights,
+                          int depth, const TracerConfig& conf);
+Color ref_raycaster_trace(const Ray& ray, KDTreeIntersection& tree_intersection, const std::vector<Light>& lights,
+                          int depth, const TracerConfig& conf);
 
 #include "lib/effects.h"
 #include "lib/raster.h"
@@ -73,7 +84,8 @@ struct Capture {
     void visit(KDTree& t) { t.serialize(*this); }
 };
 
-Triangles make_triangles(const float* verts, const float* normals, const float* diffuse, uint32_t n) {
+Triangles make_triangles(const float* verts, const float* normals, const float* diffuse, uint32_t n,
+                         const float* reflect = nullptr) {
     Triangles tris;
     tris.reserve(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -90,7 +102,14 @@ Triangles make_triangles(const float* verts, const float* normals, const float* 
             const float* c = diffuse + 4 * size_t(i);
             dif = aiColor4D{c[0], c[1], c[2], c[3]};
         }
-        tris.emplace_back(vs, ns, aiColor4D{}, dif, dif, aiColor4D{}, 0.f);
+        aiColor4D rc;
+        float rho = 0.f;
+        if (reflect) {
+            const float* q = reflect + 5 * size_t(i);
+            rc = aiColor4D{q[0], q[1], q[2], q[3]};
+            rho = q[4];
+        }
+        tris.emplace_back(vs, ns, aiColor4D{}, dif, dif, rc, rho);
     }
     return tris;
 }
@@ -118,10 +137,15 @@ struct ref_params {
     float light_position[3];
     float light_color[4];
     int32_t threads;
+    int32_t renderer;        // 0 pathtracer, 1 raytracer, 2 raycaster
+    float shadow_intensity;  // raytracer --shadow
+    float max_visibility;    // raycaster --max-visibility
 };
 
-void* ref_tree_build(const float* verts, const float* normals, const float* diffuse, uint32_t n) {
-    return new KDTree(make_triangles(verts, normals, diffuse, n));
+// reflect: n * 5 floats (reflective rgba, reflectivity) or NULL.
+void* ref_tree_build(const float* verts, const float* normals, const float* diffuse, uint32_t n,
+                     const float* reflect) {
+    return new KDTree(make_triangles(verts, normals, diffuse, n, reflect));
 }
 
 void ref_tree_free(void* t) { delete static_cast<KDTree*>(t); }
@@ -212,6 +236,8 @@ void ref_render(void* t, const ref_camera* c, const ref_params* p, float* out_rg
     conf.inverse_gamma = p->inverse_gamma;
     conf.gamma_correction_enabled = p->gamma_correction != 0;
     conf.bg_color = Color{p->background[0], p->background[1], p->background[2], 1};
+    conf.shadow_intensity = p->shadow_intensity;
+    conf.max_visibility = p->max_visibility;
 
     std::vector<Light> lights;
     if (p->n_lights > 0) {
@@ -241,7 +267,13 @@ void ref_render(void* t, const ref_camera* c, const ref_params* p, float* out_rg
                     const float dy = gen();
                     auto cam_dir = cam.raster2cam({x + dx, y + dy}, width, height);
                     Stats::instance().num_prim_rays += 1;
-                    image(x, y) += trace({cam_pos, cam_dir}, tree_intersection, lights, 0, conf);
+                    if (p->renderer == 1) {
+                        image(x, y) += ref_raytracer_trace({cam_pos, cam_dir}, tree_intersection, lights, 0, conf);
+                    } else if (p->renderer == 2) {
+                        image(x, y) += ref_raycaster_trace({cam_pos, cam_dir}, tree_intersection, lights, 0, conf);
+                    } else {
+                        image(x, y) += trace({cam_pos, cam_dir}, tree_intersection, lights, 0, conf);
+                    }
                 }
                 image(x, y) /= static_cast<float>(conf.num_pixel_samples);
                 image(x, y) = exposure(image(x, y), conf.exposure);

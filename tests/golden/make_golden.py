@@ -51,6 +51,7 @@ SCENES = {
     "sphere3": dict(kind=tg.SCENE_SPHERE_ROOM, detail=3),
     "soup2000": dict(kind=tg.SCENE_SOUP, count=2000, seed=7),
     "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8),
+    "mirror": dict(kind=tg.SCENE_MIRROR_ROOM),
 }
 
 
@@ -131,7 +132,7 @@ def scenes() -> None:
     out = {}
     for name, kw in SCENES.items():
         m = tg.make_scene(**kw)
-        t = orc.RefTree(m.vertices, m.normals, m.diffuse)
+        t = orc.RefTree(m.vertices, m.normals, m.diffuse, m.reflective)
         nodes, tris, box = t.export()
         out[f"{name}_nodes_sha"] = np.array(sha(nodes))
         out[f"{name}_tris_sha"] = np.array(sha(tris))
@@ -167,6 +168,13 @@ RENDERS = {
     "sphere3_32": dict(scene="sphere3", w=32, h=24, spp=2, depth=3, seed=11),
     "room_depth0": dict(scene="room", w=24, h=24, spp=1, depth=0, seed=3),
     "baffle8_32": dict(scene="baffle8", w=32, h=32, spp=2, depth=4, seed=5),
+    # raytracer.cpp (renderer 1) and raycaster.cpp (renderer 2)
+    "mirror_raytrace": dict(scene="mirror", w=48, h=48, spp=1, depth=3, seed=13, renderer=1),
+    "mirror_raytrace_d1_shadow08": dict(scene="mirror", w=40, h=32, spp=2, depth=1, seed=17, renderer=1,
+                                        shadow=0.8, background=(0.1, 0.2, 0.3)),
+    "room_raytrace": dict(scene="room", w=32, h=32, spp=1, depth=3, seed=19, renderer=1),
+    "room_raycast": dict(scene="room", w=40, h=40, spp=2, depth=3, seed=23, renderer=2, max_visibility=6.0),
+    "sphere3_raycast_default": dict(scene="sphere3", w=32, h=24, spp=1, depth=3, seed=29, renderer=2),
 }
 
 
@@ -174,11 +182,12 @@ def renders() -> None:
     out = {}
     for name, cfg in RENDERS.items():
         m = tg.make_scene(**SCENES[cfg["scene"]])
-        t = orc.RefTree(m.vertices, m.normals, m.diffuse)
+        t = orc.RefTree(m.vertices, m.normals, m.diffuse, m.reflective)
         img, st = t.render(m.camera.position, m.camera.trafo, ref_hfov(m), m.camera.aspect, m.light, cfg["w"],
                            cfg["h"], cfg["spp"], cfg["depth"], seed=cfg["seed"],
                            exposure=cfg.get("exposure", 1.0), gamma=cfg.get("gamma", True),
-                           background=cfg.get("background", (0.0, 0.0, 0.0)))
+                           background=cfg.get("background", (0.0, 0.0, 0.0)), renderer=cfg.get("renderer", 0),
+                           shadow_intensity=cfg.get("shadow", 0.5), max_visibility=cfg.get("max_visibility", 2.0))
         out[f"{name}_image"] = img
         out[f"{name}_rays"] = st[0]
         out[f"{name}_primary"] = st[1]

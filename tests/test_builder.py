@@ -37,7 +37,7 @@ def test_reference_test_trees(kd, name):
 
 SCENES = {"room": dict(kind=tg.SCENE_ROOM), "sphere3": dict(kind=tg.SCENE_SPHERE_ROOM, detail=3),
           "soup2000": dict(kind=tg.SCENE_SOUP, count=2000, seed=7),
-          "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8)}
+          "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8), "mirror": dict(kind=tg.SCENE_MIRROR_ROOM)}
 
 
 @pytest.mark.parametrize("name", list(SCENES))

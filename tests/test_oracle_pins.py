@@ -96,14 +96,16 @@ def test_ray_box(ray, box, expect):
 
 
 # ------------------------------------------------------- golden scene hits
-@pytest.mark.parametrize("name", ["room", "sphere3", "soup2000", "baffle8"])
+@pytest.mark.parametrize("name", ["room", "sphere3", "soup2000", "baffle8", "mirror"])
 def test_oracle_hits_match_reference(scenes, name):
     """Oracle traversal == the reference's traversal, bit for bit, on trees
-    identical to the reference's (node/triangle hashes), 8192 rays incl. zero
-    direction components and origins on vertices."""
+    identical to the reference's (node/triangle hashes, the mirror room's
+    with its reflective materials), 8192 rays incl. zero direction
+    components and origins on vertices."""
     kw = {"room": dict(kind=tg.SCENE_ROOM), "sphere3": dict(kind=tg.SCENE_SPHERE_ROOM, detail=3),
           "soup2000": dict(kind=tg.SCENE_SOUP, count=2000, seed=7),
-          "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8)}[name]
+          "baffle8": dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8),
+          "mirror": dict(kind=tg.SCENE_MIRROR_ROOM)}[name]
     tree = tg.KDTree.from_mesh(tg.make_scene(**kw))
     nodes, tris, box = tree.export()
     assert hashlib.sha256(nodes.tobytes()).hexdigest() == str(scenes[f"{name}_nodes_sha"])
@@ -123,21 +125,33 @@ RENDERS = {
     "sphere3_32": dict(scene=dict(kind=tg.SCENE_SPHERE_ROOM, detail=3), w=32, h=24, spp=2, depth=3, seed=11),
     "room_depth0": dict(scene=dict(kind=tg.SCENE_ROOM), w=24, h=24, spp=1, depth=0, seed=3),
     "baffle8_32": dict(scene=dict(kind=tg.SCENE_BAFFLE_ROOM, detail=8), w=32, h=32, spp=2, depth=4, seed=5),
+    # raytracer.cpp (renderer 1) and raycaster.cpp (renderer 2)
+    "mirror_raytrace": dict(scene=dict(kind=tg.SCENE_MIRROR_ROOM), w=48, h=48, spp=1, depth=3, seed=13,
+                            renderer=1),
+    "mirror_raytrace_d1_shadow08": dict(scene=dict(kind=tg.SCENE_MIRROR_ROOM), w=40, h=32, spp=2, depth=1,
+                                        seed=17, renderer=1, shadow=0.8, background=(0.1, 0.2, 0.3)),
+    "room_raytrace": dict(scene=dict(kind=tg.SCENE_ROOM), w=32, h=32, spp=1, depth=3, seed=19, renderer=1),
+    "room_raycast": dict(scene=dict(kind=tg.SCENE_ROOM), w=40, h=40, spp=2, depth=3, seed=23, renderer=2,
+                         max_visibility=6.0),
+    "sphere3_raycast_default": dict(scene=dict(kind=tg.SCENE_SPHERE_ROOM, detail=3), w=32, h=24, spp=1, depth=3,
+                                    seed=29, renderer=2),
 }
 
 
 @pytest.mark.parametrize("name", list(RENDERS))
 def test_oracle_render_matches_reference(renders, name):
     """trace() restated == the reference's trace() under the same per-path
-    seeds: identical ray counts; images bit-identical on the same libm (x86-64
-    glibc here), within 1e-6 elsewhere."""
+    seeds (path tracer, raytracer and raycaster): identical ray counts; images
+    bit-identical on the same libm (x86-64 glibc here), within 1e-6
+    elsewhere."""
     cfg = RENDERS[name]
     m = tg.make_scene(**cfg["scene"])
     nodes, tris, box = tg.KDTree.from_mesh(m).export()
     sc = orc.Scene(nodes, tris, box)
     img, st = sc.render(m.camera, m.light, cfg["w"], cfg["h"], cfg["spp"], cfg["depth"], seed=cfg["seed"],
                         exposure=cfg.get("exposure", 1.0), gamma=cfg.get("gamma", True),
-                        background=cfg.get("background", (0.0, 0.0, 0.0)))
+                        background=cfg.get("background", (0.0, 0.0, 0.0)), renderer=cfg.get("renderer", 0),
+                        shadow_intensity=cfg.get("shadow", 0.5), max_visibility=cfg.get("max_visibility", 2.0))
     gold = renders[f"{name}_image"]
     assert int(st[0]) == int(renders[f"{name}_rays"])
     assert int(st[1]) == int(renders[f"{name}_primary"])

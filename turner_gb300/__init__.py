@@ -46,6 +46,7 @@ SCENE_SPHERE_ROOM = 1
 SCENE_SOUP = 2
 SCENE_BAFFLE_ROOM = 3
 SCENE_BAFFLE_SPHERE = 4
+SCENE_MIRROR_ROOM = 5
 
 TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
@@ -162,6 +163,8 @@ def _lib() -> C.CDLL:
         "turner_mesh_vertices": (C.POINTER(C.c_float), [_P]),
         "turner_mesh_normals": (C.POINTER(C.c_float), [_P]),
         "turner_mesh_diffuse": (C.POINTER(C.c_float), [_P]),
+        "turner_mesh_reflective": (C.POINTER(C.c_float), [_P]),
+        "turner_kdtree_set_reflective": (C.c_int, [_P, _P]),
         "turner_mesh_camera": (None, [_P, C.POINTER(Camera), C.POINTER(C.c_float)]),
         "turner_mesh_light": (C.c_int, [_P, C.POINTER(Light)]),
         "turner_mesh_free": (None, [_P]),
@@ -195,6 +198,7 @@ class Mesh:
     camera: Camera
     hfov: float
     light: Light | None
+    reflective: np.ndarray | None = None   # (n, 5) float32: reflective rgba, reflectivity
 
     @property
     def n_triangles(self) -> int:
@@ -210,6 +214,7 @@ def make_scene(kind: int, detail: int = 0, count: int = 0, seed: int = 1, aspect
         v = np.ctypeslib.as_array(lib.turner_mesh_vertices(h), (n, 9)).copy()
         nr = np.ctypeslib.as_array(lib.turner_mesh_normals(h), (n, 9)).copy()
         d = np.ctypeslib.as_array(lib.turner_mesh_diffuse(h), (n, 4)).copy()
+        rf = np.ctypeslib.as_array(lib.turner_mesh_reflective(h), (n, 5)).copy()
         cam = Camera()
         hfov = C.c_float()
         lib.turner_mesh_camera(h, C.byref(cam), C.byref(hfov))
@@ -217,7 +222,7 @@ def make_scene(kind: int, detail: int = 0, count: int = 0, seed: int = 1, aspect
         nl = lib.turner_mesh_light(h, C.byref(light))
     finally:
         lib.turner_mesh_free(h)
-    return Mesh(v, nr, d, cam, hfov.value, light if nl else None)
+    return Mesh(v, nr, d, cam, hfov.value, light if nl else None, rf if rf.any() else None)
 
 
 def make_rays(n: int, box, seed: int) -> tuple[np.ndarray, np.ndarray]:
@@ -264,7 +269,17 @@ class KDTree:
 
     @classmethod
     def from_mesh(cls, mesh: Mesh, threads: int = 0, cache_dir: str | None = None) -> "KDTree":
-        return cls(mesh.vertices, mesh.normals, mesh.diffuse, threads, cache_dir)
+        t = cls(mesh.vertices, mesh.normals, mesh.diffuse, threads, cache_dir)
+        if mesh.reflective is not None:
+            t.set_reflective(mesh.reflective)
+        return t
+
+    def set_reflective(self, reflective: np.ndarray) -> None:
+        """Reflective colour (rgba) and reflectivity per triangle, (n, 5)."""
+        r = np.ascontiguousarray(reflective, np.float32).reshape(-1, 5)
+        if r.shape[0] != self.num_triangles():
+            raise ValueError("one row per triangle")
+        _check(_lib().turner_kdtree_set_reflective(self._h, _ptr(r)), "turner_kdtree_set_reflective")
 
     @classmethod
     def load(cls, path, key: int = 0) -> "KDTree":

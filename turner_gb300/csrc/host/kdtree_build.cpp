@@ -419,6 +419,15 @@ Box triangle_box(const turner_triangle& t) {
 
 extern "C" {
 
+int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective) {
+    if (!tree || !reflective) return TURNER_ERR_INVALID_ARG;
+    for (size_t i = 0; i < tree->tris.size(); ++i) {
+        std::memcpy(tree->tris[i].reflective, reflective + 5 * i, 4 * sizeof(float));
+        tree->tris[i].reflectivity = reflective[5 * i + 4];
+    }
+    return TURNER_OK;
+}
+
 int turner_kdtree_build(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris,
                         int threads, turner_kdtree** out) {
     if (!vertices || !out || n_tris == 0) return TURNER_ERR_INVALID_ARG;

@@ -18,6 +18,7 @@
 
 struct turner_mesh {
     std::vector<float> verts, normals, diffuse;
+    std::vector<float> reflect;   // per triangle: reflective colour (4), reflectivity
     turner_camera cam{};
     float hfov = 0;
     int n_lights = 0;
@@ -53,6 +54,7 @@ constexpr Color4 kGreen{0.14f, 0.45f, 0.09f, 1.f};
 
 struct Builder {
     turner_mesh* m;
+    float refl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};   // material of the triangles added next
 
     void tri(D3 a, D3 b, D3 c, D3 na, D3 nb, D3 nc, Color4 col) {
         const D3 p[3] = {a, b, c};
@@ -69,6 +71,7 @@ struct Builder {
         m->diffuse.push_back(col.g);
         m->diffuse.push_back(col.b);
         m->diffuse.push_back(col.a);
+        for (float r : refl) m->reflect.push_back(r);
     }
     void flat_tri(D3 a, D3 b, D3 c, D3 n, Color4 col) { tri(a, b, c, n, n, n, col); }
 
@@ -321,6 +324,19 @@ int turner_scene_make(int kind, uint32_t detail, uint32_t count, uint64_t seed, 
         inner_boxes(b);
         ceiling_quad(b);
         break;
+    case TURNER_SCENE_MIRROR_ROOM: {
+        // the room with reflective boxes, for the Whitted raytracer
+        // (raytracer.cpp reads reflectivity and the reflective colour)
+        room_walls(b, 1);
+        const float short_box[5] = {1.f, 1.f, 1.f, 1.f, 0.3f}, tall_box[5] = {0.9f, 0.9f, 0.95f, 1.f, 0.85f};
+        std::memcpy(b.refl, short_box, sizeof(b.refl));
+        b.box({3.70, 0.825, -1.90}, {0.825, 0.825, 0.825}, kCos17, -kSin17, kWhite);
+        std::memcpy(b.refl, tall_box, sizeof(b.refl));
+        b.box({1.85, 1.650, -3.70}, {0.825, 1.650, 0.825}, kCos17, kSin17, kWhite);
+        std::memset(b.refl, 0, sizeof(b.refl));
+        ceiling_quad(b);
+        break;
+    }
     case TURNER_SCENE_SPHERE_ROOM:
         if (detail > 9) { delete m; return TURNER_ERR_TOO_LARGE; }
         room_walls(b, 1);
@@ -360,6 +376,7 @@ uint32_t turner_mesh_num_triangles(const turner_mesh* m) { return m ? static_cas
 const float* turner_mesh_vertices(const turner_mesh* m) { return m ? m->verts.data() : nullptr; }
 const float* turner_mesh_normals(const turner_mesh* m) { return m ? m->normals.data() : nullptr; }
 const float* turner_mesh_diffuse(const turner_mesh* m) { return m ? m->diffuse.data() : nullptr; }
+const float* turner_mesh_reflective(const turner_mesh* m) { return m ? m->reflect.data() : nullptr; }
 
 void turner_mesh_camera(const turner_mesh* m, turner_camera* cam, float* hfov) {
     if (!m) return;
