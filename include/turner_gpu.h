@@ -134,7 +134,22 @@ typedef struct turner_job {
     int32_t linear_output;        /* 1: write the per-pixel mean radiance
                                      without exposure and gamma (for error
                                      measurements against converged images) */
+    int32_t renderer;             /* TURNER_RENDERER_*: which trace() plug-in */
+    float shadow_intensity;       /* raytracer --shadow (config.h: 0.5)       */
+    float max_visibility;         /* raycaster --max-visibility (config.h: 2) */
 } turner_job;
+
+/* The reference links one trace() per executable (trace.h:23-25):
+ *   PATH      pathtracer.cpp:14-102 (default)
+ *   RAYTRACE  raytracer.cpp:5-67: Lambertian direct light, mirror bounces
+ *             up to max_depth, shadows darken by shadow_intensity; needs
+ *             exactly one light (the reference reads lights.front())
+ *   RAYCAST   raycaster.cpp:6-24: diffuse colour, alpha = 1 - r /
+ *             max_visibility clamped to [0, 1]; only hits count as rays
+ * RAYTRACE and RAYCAST ignore sampling and monte_carlo_samples. */
+#define TURNER_RENDERER_PATH 0
+#define TURNER_RENDERER_RAYTRACE 1
+#define TURNER_RENDERER_RAYCAST 2
 
 /* Largest -m. */
 #define TURNER_MAX_MC 64

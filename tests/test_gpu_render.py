@@ -207,3 +207,69 @@ def test_tree_file_upload_and_cli_cache(ctx, tmp_path):
     assert r1.returncode == 0 and r2.returncode == 0, r1.stderr + r2.stderr
     assert "Loaded kd-tree" not in r1.stderr and "Loaded kd-tree" in r2.stderr
     assert r1.stdout == r2.stdout and r1.stdout.startswith("P3\n32 32\n255\n")
+
+
+CLASSIC = {
+    # golden name: (scene, job arguments)
+    "mirror_raytrace": (dict(kind=tg.SCENE_MIRROR_ROOM),
+                        dict(width=48, height=48, pixel_samples=1, max_depth=3, seed=13,
+                             renderer=tg.RENDERER_RAYTRACE)),
+    "mirror_raytrace_d1_shadow08": (dict(kind=tg.SCENE_MIRROR_ROOM),
+                                    dict(width=40, height=32, pixel_samples=2, max_depth=1, seed=17,
+                                         renderer=tg.RENDERER_RAYTRACE, shadow_intensity=0.8,
+                                         background=(0.1, 0.2, 0.3))),
+    "room_raytrace": (dict(kind=tg.SCENE_ROOM), dict(width=32, height=32, pixel_samples=1, max_depth=3, seed=19,
+                                                     renderer=tg.RENDERER_RAYTRACE)),
+    "room_raycast": (dict(kind=tg.SCENE_ROOM), dict(width=40, height=40, pixel_samples=2, max_depth=3, seed=23,
+                                                    renderer=tg.RENDERER_RAYCAST, max_visibility=6.0)),
+    "sphere3_raycast_default": (dict(kind=tg.SCENE_SPHERE_ROOM, detail=3),
+                                dict(width=32, height=24, pixel_samples=1, max_depth=3, seed=29,
+                                     renderer=tg.RENDERER_RAYCAST)),
+}
+
+
+@pytest.mark.parametrize("name", list(CLASSIC))
+def test_raytracer_and_raycaster_match_reference(ctx, name):
+    """raytracer.cpp / raycaster.cpp through the wavefront == the reference's
+    own renders (tests/golden/ref_renders.npz): the same ray count exactly
+    (no sampling: every ray is the reference's ray) and the image within the
+    render tolerance."""
+    g = dict(np.load(GOLD / "ref_renders.npz"))
+    scene_kw, job_kw = CLASSIC[name]
+    m = tg.make_scene(**scene_kw)
+    sid = ctx.upload_tree(tg.KDTree.from_mesh(m))
+    job = tg.make_job(sid, m, **job_kw)
+    (img,), (st,) = ctx.render([job])
+    check_close(img, g[f"{name}_image"])
+    assert int(st.rays) == int(g[f"{name}_rays"])
+    assert int(st.primary_rays) == int(g[f"{name}_primary"])
+
+
+def test_renderers_share_a_batch(ctx):
+    """A path-traced, a raytraced and a raycast job in one batch: each image
+    is bit-identical to the same job rendered alone."""
+    m = tg.make_scene(tg.SCENE_MIRROR_ROOM)
+    sid = ctx.upload_tree(tg.KDTree.from_mesh(m))
+    jobs = [tg.make_job(sid, m, 24, 24, pixel_samples=2, max_depth=3, seed=1),
+            tg.make_job(sid, m, 32, 16, pixel_samples=1, max_depth=4, seed=2, renderer=tg.RENDERER_RAYTRACE),
+            tg.make_job(sid, m, 16, 16, pixel_samples=3, seed=3, renderer=tg.RENDERER_RAYCAST, max_visibility=5.0)]
+    imgs, stats = ctx.render(jobs)
+    for job, img, st in zip(jobs, imgs, stats):
+        (alone,), (sa,) = ctx.render([job])
+        assert np.array_equal(img, alone)
+        assert st.rays == sa.rays
+
+
+def test_renderer_arguments_are_checked(ctx):
+    m = tg.make_scene(tg.SCENE_ROOM)
+    sid = ctx.upload_tree(tg.KDTree.from_mesh(m))
+    bad = [tg.make_job(sid, m, 8, 8, renderer=3),
+           tg.make_job(sid, m, 8, 8, renderer=tg.RENDERER_RAYTRACE, shadow_intensity=1.5),
+           tg.make_job(sid, m, 8, 8, renderer=tg.RENDERER_RAYCAST, max_visibility=-1.0)]
+    nolight = tg.make_job(sid, m, 8, 8, renderer=tg.RENDERER_RAYTRACE)
+    nolight.n_lights = 0
+    bad.append(nolight)
+    for job in bad:
+        with pytest.raises(tg.TurnerError) as e:
+            ctx.render([job])
+        assert e.value.status == tg.ERR_INVALID_ARG

@@ -51,6 +51,7 @@ SCENE_MIRROR_ROOM = 5
 TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
 GRAPH_AUTO, GRAPH_ALWAYS, GRAPH_NEVER = 0, 1, 2
+RENDERER_PATH, RENDERER_RAYTRACE, RENDERER_RAYCAST = 0, 1, 2
 KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect", "k_guide_features",
                 "k_mlp_forward", "guide_train")
 KERNEL_KINDS = len(KERNEL_NAMES)
@@ -78,7 +79,8 @@ class Job(C.Structure):
                 ("exposure", C.c_float), ("inverse_gamma", C.c_float), ("gamma_correction", C.c_int32),
                 ("background", C.c_float * 3), ("seed", C.c_uint64), ("n_lights", C.c_int32),
                 ("light", Light), ("camera", Camera), ("sampling", C.c_int32), ("traversal", C.c_int32),
-                ("linear_output", C.c_int32)]
+                ("linear_output", C.c_int32), ("renderer", C.c_int32), ("shadow_intensity", C.c_float),
+                ("max_visibility", C.c_float)]
 
 
 class Tuning(C.Structure):
@@ -578,8 +580,10 @@ def look_at_camera(position, target, aspect: float, vfov_deg: float = 40.0, up=(
 def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, pixel_samples: int = 1,
              max_depth: int = 3, monte_carlo_samples: int = 1, seed: int = 1, exposure: float = 1.0,
              inverse_gamma: float = 0.454545, gamma_correction: bool = True, background=(0.0, 0.0, 0.0),
-             sampling: int = SAMPLING_UNIFORM, traversal: int = TRAVERSAL_PARITY) -> Job:
-    """A job with the reference's defaults (config.h, pathtracer.h)."""
+             sampling: int = SAMPLING_UNIFORM, traversal: int = TRAVERSAL_PARITY, renderer: int = RENDERER_PATH,
+             shadow_intensity: float = 0.5, max_visibility: float = 2.0) -> Job:
+    """A job with the reference's defaults (config.h, pathtracer.h,
+    raytracer.h, raycaster.h)."""
     j = Job()
     j.scene_id = scene_id
     j.width = width
@@ -599,6 +603,9 @@ def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, p
     j.camera = mesh.camera
     j.sampling = sampling
     j.traversal = traversal
+    j.renderer = renderer
+    j.shadow_intensity = shadow_intensity
+    j.max_visibility = max_visibility
     return j
 
 

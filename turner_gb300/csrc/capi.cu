@@ -44,7 +44,7 @@ struct DevBuf {
 
 struct SceneStore {
     bool live = false;
-    DevBuf nodes, tri, shade;
+    DevBuf nodes, tri, shade, refl;
     SceneView view{};
 };
 
@@ -61,7 +61,7 @@ struct turner_ctx {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
     // render workspace
-    DevBuf L, qa[4], qb[4], hits, shq[3], shjob, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
+    DevBuf L, qa[4], qb[4], hits, shq[3], shjob, shaux, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
     uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
     uint64_t acc_samples = 0, acc_passes = 0;
     int graph_mode = TURNER_GRAPH_AUTO;
@@ -211,12 +211,15 @@ void fill_job(const turner_job& j, const SceneView& sc, JobDesc& d) {
     d.inv_gamma = j.inverse_gamma;
     d.gamma = j.gamma_correction;
     d.tone_map = 1;
+    d.renderer = j.renderer;
+    d.shadow_intensity = j.shadow_intensity;
+    d.max_visibility = j.max_visibility;
 }
 
 // Rays of one path at its widest level: M^max_depth for the branching
 // estimator (-m M > 1), else 1; 0 if that exceeds 2^26.
 uint64_t branch_width(const turner_job& j) {
-    if (j.monte_carlo_samples <= 1) return 1;
+    if (j.monte_carlo_samples <= 1 || j.renderer != TURNER_RENDERER_PATH) return 1;
     uint64_t w = 1;
     for (int d = 0; d < j.max_depth; ++d) {
         w *= static_cast<uint64_t>(j.monte_carlo_samples);
@@ -238,6 +241,14 @@ int check_job(turner_ctx* ctx, const turner_job& j) {
         return TURNER_ERR_INVALID_ARG;
     if (j.sampling == TURNER_SAMPLING_GUIDED && !ctx->guide) return TURNER_ERR_INVALID_ARG;
     if (j.traversal != TURNER_TRAVERSAL_PARITY && j.traversal != TURNER_TRAVERSAL_FAST) return TURNER_ERR_INVALID_ARG;
+    if (j.renderer < TURNER_RENDERER_PATH || j.renderer > TURNER_RENDERER_RAYCAST) return TURNER_ERR_INVALID_ARG;
+    if (j.renderer != TURNER_RENDERER_PATH) {
+        // TracerConfig::check (config.h:125-132); the raytracer reads lights.front()
+        if (!(j.shadow_intensity >= 0.f && j.shadow_intensity <= 1.f) || !(j.max_visibility >= 0.f))
+            return TURNER_ERR_INVALID_ARG;
+        if (j.renderer == TURNER_RENDERER_RAYTRACE && j.n_lights != 1) return TURNER_ERR_INVALID_ARG;
+        if (j.sampling == TURNER_SAMPLING_GUIDED) return TURNER_ERR_INVALID_ARG;
+    }
     if (uint64_t(j.width) * j.height > (1ull << 31)) return TURNER_ERR_TOO_LARGE;
     if (j.max_depth > 64) return TURNER_ERR_TOO_LARGE;
     return TURNER_OK;
@@ -333,7 +344,10 @@ int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes
 
     auto sc = std::unique_ptr<SceneStore>(new (std::nothrow) SceneStore);
     if (!sc) return TURNER_ERR_OUT_OF_MEMORY;
-    std::vector<float4> tri(4 * size_t(n_tris)), shade(4 * size_t(n_tris));
+    std::vector<float4> tri(4 * size_t(n_tris)), shade(4 * size_t(n_tris)), refl;
+    bool any_reflective = false;
+    for (uint32_t i = 0; i < n_tris && !any_reflective; ++i) any_reflective = tris[i].reflectivity > 0.f;
+    if (any_reflective) refl.resize(n_tris);
     for (uint32_t i = 0; i < n_tris; ++i) {
         const turner_triangle& t = tris[i];
         tri[4 * i + 0] = make_float4(t.vertices[0][0], t.vertices[0][1], t.vertices[0][2], t.uv);
@@ -343,7 +357,8 @@ int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes
         shade[4 * i + 0] = make_float4(t.normals[0][0], t.normals[0][1], t.normals[0][2], t.diffuse[0]);
         shade[4 * i + 1] = make_float4(t.normals[1][0], t.normals[1][1], t.normals[1][2], t.diffuse[1]);
         shade[4 * i + 2] = make_float4(t.normals[2][0], t.normals[2][1], t.normals[2][2], t.diffuse[2]);
-        shade[4 * i + 3] = make_float4(t.diffuse[3], 0.f, 0.f, 0.f);
+        shade[4 * i + 3] = make_float4(t.diffuse[3], t.reflectivity, 0.f, 0.f);
+        if (any_reflective) refl[i] = make_float4(t.reflective[0], t.reflective[1], t.reflective[2], t.reflective[3]);
     }
     TURNER_CK(sc->nodes.ensure(sizeof(uint64_t) * n_nodes));
     TURNER_CK(sc->tri.ensure(sizeof(float4) * tri.size()));
@@ -352,11 +367,17 @@ int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes
     TURNER_CK(cudaMemcpyAsync(sc->tri.p, tri.data(), sizeof(float4) * tri.size(), cudaMemcpyHostToDevice, ctx->stream));
     TURNER_CK(cudaMemcpyAsync(sc->shade.p, shade.data(), sizeof(float4) * shade.size(), cudaMemcpyHostToDevice,
                               ctx->stream));
+    if (any_reflective) {
+        TURNER_CK(sc->refl.ensure(sizeof(float4) * refl.size()));
+        TURNER_CK(cudaMemcpyAsync(sc->refl.p, refl.data(), sizeof(float4) * refl.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    }
     TURNER_CK(cudaStreamSynchronize(ctx->stream));
     SceneView& v = sc->view;
     v.nodes = sc->nodes.as<uint2>();
     v.tri = sc->tri.as<float4>();
     v.shade = sc->shade.as<float4>();
+    v.refl = any_reflective ? sc->refl.as<float4>() : nullptr;
     for (int k = 0; k < 3; ++k) {
         v.lo[k] = box[k];
         v.hi[k] = box[3 + k];
@@ -378,6 +399,7 @@ int turner_free_scene(turner_ctx* ctx, uint32_t scene_id) {
     sc.nodes.release();
     sc.tri.release();
     sc.shade.release();
+    sc.refl.release();
     sc.live = false;
     return TURNER_OK;
 }
@@ -482,6 +504,8 @@ struct Batch {
     uint32_t max_height = 0;         // deepest traversal stack any scene needs
     bool guided = false;             // some job samples with the learned proposal
     bool branching = false;          // some job has -m > 1 (radiance is added atomically)
+    bool has_path = false;           // some job uses the path tracer
+    bool has_classic = false;        // some job uses the raytracer or the raycaster
 };
 
 int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4* const* outs, bool tone_map,
@@ -502,6 +526,8 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
         load += uint64_t(d.width) * d.height * d.spp * width[j];
         max_load = std::max<uint64_t>(max_load, uint64_t(d.spp) * width[j]);
         if (width[j] > 1) b.branching = true;
+        if (d.renderer == TURNER_RENDERER_PATH) b.has_path = true;
+        else b.has_classic = true;
         b.levels = std::max(b.levels, d.max_depth + 1);
         if (jobs[j].scene_id != jobs[0].scene_id) b.single_scene = false;
         b.max_height = std::max(b.max_height, d.sc.height);
@@ -548,6 +574,7 @@ int ensure_workspace(turner_ctx* ctx, const Batch& b) {
     TURNER_CK(ctx->qa[3].ensure(sizeof(uint2) * cap));
     TURNER_CK(ctx->qb[3].ensure(sizeof(uint2) * cap));
     TURNER_CK(ctx->shjob.ensure(sizeof(uint32_t) * cap));
+    if (b.has_classic) TURNER_CK(ctx->shaux.ensure(sizeof(uint32_t) * cap));
     TURNER_CK(ctx->hits.ensure(sizeof(Hit) * cap));
     TURNER_CK(ctx->counters.ensure(sizeof(uint32_t) * 4 * size_t(b.levels + 1) * b.chunks.size()));
     TURNER_CK(ctx->jobtab.ensure(sizeof(JobDesc) * b.table.size()));
@@ -599,7 +626,7 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                        ctx->r_fcp.as<float>(), ctx->r_count.as<uint32_t>(), ctx->guide_records, 0};
     }
     ShadowQueue sh{ctx->shq[0].as<float4>(), ctx->shq[1].as<float4>(), ctx->shq[2].as<float4>(),
-                   ctx->shjob.as<uint32_t>(), nullptr};
+                   ctx->shjob.as<uint32_t>(), nullptr, b.has_classic ? ctx->shaux.as<uint32_t>() : nullptr};
     for (size_t ci = 0; ci < b.chunks.size(); ++ci) {
         const Chunk& c = b.chunks[ci];
         uint32_t* cnt = counters + stride * ci;   // [queued rays | shadow rays | trace work | shadow work]
@@ -639,14 +666,19 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                 }
                 if (gs != TURNER_OK) return gs;
             }
-            {
+            if (b.has_path) {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
                 launch_shade(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts, gq,
-                             recs, c.n_rays, ctx->stream);
+                             recs, c.n_rays, b.has_classic, ctx->stream);
+            }
+            if (b.has_classic) {
+                KernelTimer kt(ctx, TURNER_KERNEL_SHADE);
+                launch_shade_classic(jobs, depth, cur, ctx->hits.as<Hit>(), nxt, sh, ctx->L.as<float4>(), job_counts,
+                                     c.n_rays, ctx->stream);
             }
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_SHADOW);
-                launch_shadow(single, jobs, sh, ctx->L.as<float4>(), c.n_rays, b.branching, shadow_cfg,
+                launch_shadow(single, jobs, sh, ctx->L.as<float4>(), c.n_rays, b.branching, nxt.T, shadow_cfg,
                               ctx->stream);
             }
             std::swap(cur, nxt);

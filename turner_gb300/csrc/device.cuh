@@ -30,7 +30,8 @@ constexpr int kStackCap = 128;              // entries; scenes deeper than this 
 struct SceneView {
     const uint2* nodes;
     const float4* tri;
-    const float4* shade;
+    const float4* shade;   // {n0, d.r} {n1, d.g} {n2, d.b} {d.a, reflectivity, 0, 0}
+    const float4* refl;    // reflective colour per triangle; null when no triangle reflects
     float lo[3], hi[3];
     uint32_t n_nodes, n_tris, height;
 };

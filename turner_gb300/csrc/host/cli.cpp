@@ -37,13 +37,17 @@ Pathtracer options:
 
 GB300 options:
   --seed=<int>                      Stream seed base [default: 1].
+  --renderer=<name>                 trace() plug-in: path (pathtracer), raytrace
+                                    (raytracer) or raycast (raycaster) [default: path].
+  --shadow=<float>                  Raytracer: intensity of shadow [default: 0.5].
+  --max-visibility=<float>          Raycaster: any object farther away is dark [default: 2.0].
   --cosine                          Cosine-weighted bounces instead of uniform.
   --fast                            Early-exit closest-hit traversal for bounce rays.
   --device=<int>                    CUDA device [default: 0].
   --kdtree-cache=<dir>              Directory of content-keyed kd-tree files: load the
                                     scene's tree from it, or build and store it.
 
-Scenes: room | sphere[:DETAIL] | soup:COUNT[:SEED] | baffle[:DETAIL] | baffle-sphere[:DETAIL]
+Scenes: room | sphere[:DETAIL] | soup:COUNT[:SEED] | baffle[:DETAIL] | baffle-sphere[:DETAIL] | mirror
 )";
 
 struct Options {
@@ -60,6 +64,8 @@ struct Options {
     int mc = 8;
     uint64_t seed = 1;
     bool cosine = false, fast = false;
+    int renderer = TURNER_RENDERER_PATH;
+    float shadow = 0.5f, max_visibility = 2.f;
     int device = 0;
     std::string kdtree_cache;
 };
@@ -116,6 +122,14 @@ int parse(int argc, char** argv, Options& o) {
         else if (take(i, argc, argv, "-m", "--monte-carlo-samples", v)) o.mc = std::stoi(v);
         else if (take(i, argc, argv, nullptr, "--seed", v)) o.seed = std::stoull(v);
         else if (a == "--cosine") o.cosine = true;
+        else if (take(i, argc, argv, nullptr, "--shadow", v)) o.shadow = std::stof(v);
+        else if (take(i, argc, argv, nullptr, "--max-visibility", v)) o.max_visibility = std::stof(v);
+        else if (take(i, argc, argv, nullptr, "--renderer", v)) {
+            if (v == "path") o.renderer = TURNER_RENDERER_PATH;
+            else if (v == "raytrace") o.renderer = TURNER_RENDERER_RAYTRACE;
+            else if (v == "raycast") o.renderer = TURNER_RENDERER_RAYCAST;
+            else return 2;
+        }
         else if (a == "--fast") o.fast = true;
         else if (take(i, argc, argv, nullptr, "--device", v)) o.device = std::stoi(v);
         else if (take(i, argc, argv, nullptr, "--kdtree-cache", v)) o.kdtree_cache = v;
@@ -124,7 +138,7 @@ int parse(int argc, char** argv, Options& o) {
     }
     // TracerConfig::check (config.h:120-127) and Config::check (config.h:30-34)
     if (o.scene.empty() || !(o.aspect > 0) || o.exposure < 0 || o.depth <= 0 || o.pixel_samples < 1 || o.mc < 0 ||
-        o.width < 1)
+        o.width < 1 || !(o.shadow >= 0.f && o.shadow <= 1.f) || !(o.max_visibility >= 0.f))
         return 2;
     return 0;
 }
@@ -146,6 +160,7 @@ int make_scene(const std::string& spec, float aspect, turner_mesh** mesh) {
     if (name == "soup") return turner_scene_make(TURNER_SCENE_SOUP, 0, num(1, 10000), num(2, 1), aspect, mesh);
     if (name == "baffle") return turner_scene_make(TURNER_SCENE_BAFFLE_ROOM, num(1, 64), 0, 1, aspect, mesh);
     if (name == "baffle-sphere") return turner_scene_make(TURNER_SCENE_BAFFLE_SPHERE, num(1, 7), 64, 1, aspect, mesh);
+    if (name == "mirror") return turner_scene_make(TURNER_SCENE_MIRROR_ROOM, 0, 0, 1, aspect, mesh);
     return TURNER_ERR_INVALID_ARG;
 }
 
@@ -179,6 +194,7 @@ int main(int argc, char** argv) {
         return 1;
     }
     if (from_cache) std::cerr << "Loaded kd-tree from " << o.kdtree_cache << std::endl;
+    turner_kdtree_set_reflective(tree, turner_mesh_reflective(mesh));   // the raytracer's materials
     const double tree_ms = std::chrono::duration<double, std::milli>(clock::now() - t_tree).count();
     std::cerr << "KDTree runtime: " << static_cast<long>(tree_ms) << std::endl;
     const double load_s = std::chrono::duration<double>(clock::now() - t_load).count();
@@ -215,6 +231,9 @@ int main(int argc, char** argv) {
     job.camera = cam;
     job.sampling = o.cosine ? TURNER_SAMPLING_COSINE : TURNER_SAMPLING_UNIFORM;
     job.traversal = o.fast ? TURNER_TRAVERSAL_FAST : TURNER_TRAVERSAL_PARITY;
+    job.renderer = o.renderer;
+    job.shadow_intensity = o.shadow;
+    job.max_visibility = o.max_visibility;
     if (o.verbose) {
         std::cerr << "Scene: " << o.scene << "\nImage: " << job.width << "x" << job.height << "\nSamples: "
                   << job.pixel_samples << "\nMax depth: " << job.max_depth << std::endl;

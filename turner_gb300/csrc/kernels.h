@@ -49,7 +49,13 @@ struct ShadowQueue {
     float4* c;        // contribution added to the path if the light is visible
     uint32_t* job;    // job index
     uint32_t* count;
+    uint32_t* aux;    // batches with raytracer jobs: kAuxPath, kAuxNoChild or the
+                      // queue slot of the mirror ray spawned at the same hit
 };
+
+constexpr uint32_t kAuxPath = 0xFFFFFFFEu;      // path-tracer entry: a blocked ray adds nothing
+constexpr uint32_t kAuxNoChild = 0xFFFFFFFFu;   // raytracer entry without a mirror ray
+constexpr int kRendererPath = 0, kRendererRaytrace = 1, kRendererRaycast = 2;
 
 // One image of a batch, resident in device memory (the job table).
 struct JobDesc {
@@ -67,6 +73,8 @@ struct JobDesc {
     int32_t sampling, traversal;
     float exposure, inv_gamma;
     int32_t gamma, tone_map;
+    int32_t renderer;
+    float shadow_intensity, max_visibility;
     uint64_t pixel_offset;   // first pixel of this job in the batch's pixel space
     uint64_t path_offset;    // first path of this job in the batch's path space
     float4* out;             // output image (device)
@@ -111,14 +119,20 @@ void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& 
 // when no job of the batch samples with the learned proposal).
 void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
                   const ShadowQueue& sh, float4* L, unsigned long long* job_counts, const GuideQueue& gq,
-                  const Records& recs, uint32_t capacity, cudaStream_t stream);
+                  const Records& recs, uint32_t capacity, bool mixed, cudaStream_t stream);
 // Network inputs for the hits of guided jobs that will bounce (zeros elsewhere).
+// The raytracer's and raycaster's shading (raytracer.cpp:5-67,
+// raycaster.cpp:6-24) of the entries of their jobs; k_shade skips those.
+void launch_shade_classic(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
+                          const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
+                          cudaStream_t stream);
 void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, const Hit* hits, float* feat,
                            uint32_t capacity, cudaStream_t stream);
 // atomic_l: add to L atomically (batches with -m > 1, where several shadow
-// rays of one path are in the queue at once).
+// rays of one path are in the queue at once). next_T: throughput of the next
+// ray queue, which blocked raytracer shadow rays darken (sh.aux non-null).
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
-                   bool atomic_l, const TraverseCfg& cfg, cudaStream_t stream);
+                   bool atomic_l, float4* next_T, const TraverseCfg& cfg, cudaStream_t stream);
 void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream);
 // acc[p] += (double) sum of the chunk's sample radiance for pixel p (linear)
 void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, double4* acc,

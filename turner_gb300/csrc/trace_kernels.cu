@@ -190,17 +190,20 @@ __global__ void __launch_bounds__(kBlock) k_guide_features(const JobDesc* __rest
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
 __device__ __forceinline__ float4 scale4(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
 __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) { return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
 
 __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jobs, int depth, RayQueue in,
                                                   const Hit* __restrict__ hits, RayQueue out, ShadowQueue sh,
                                                   float4* __restrict__ L, unsigned long long* __restrict__ job_counts,
-                                                  GuideQueue gq, Records recs) {
+                                                  GuideQueue gq, Records recs, bool mixed) {
     const uint32_t n = *in.count;
     const uint32_t stride = gridDim.x * blockDim.x;
     // warp-uniform loop so every lane reaches the ballots
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
         const uint32_t i = base + lane_id();
-        const bool valid = i < n;
+        // mixed: the batch also holds raytracer / raycaster jobs, whose entries
+        // k_shade_classic shades
+        const bool valid = i < n && (!mixed || jobs[__float_as_uint(in.d[i].w)].renderer == kRendererPath);
         bool emit_shadow = false, emit_bounce = false;
         float4 sh_o, sh_d, sh_c, b_o, b_d, b_T;
         uint2 b_rng;
@@ -363,6 +366,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
             sh.d[si] = sh_d;
             sh.c[si] = sh_c;
             sh.job[si] = jidx;
+            if (sh.aux) sh.aux[si] = kAuxPath;
         }
         uint32_t b_rec = kNoRecord;
         if (recs.count) {
@@ -428,6 +432,135 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
     }
 }
 
+// The other two trace() plug-ins on the same queues.
+//   raycaster.cpp:6-24   hit: the diffuse colour with alpha 1 - r / max_visibility
+//                        clamped to [0, 1], counted as a ray; miss: background
+//   raytracer.cpp:5-67   every call is a ray (also the mirror call one past max
+//                        depth, which returns 0); hit: Lambertian direct light
+//                        cos * C * I (lib/lambertian.h:15-19) weighted by 1 -
+//                        reflectivity when the triangle reflects, plus a mirror
+//                        ray d - 2 (n.d) n with throughput reflectivity *
+//                        reflective colour; then a shadow ray toward the light.
+// In this forward form the shadow ray of a hit carries the hit's direct
+// contribution and the queue slot of its mirror ray: when it is blocked
+// (a hit with r < |light - p2|), the shadow kernel adds the contribution
+// darkened as c - c * shadow_intensity and darkens the mirror ray's
+// throughput the same way (the reference's color -= color * shadow_intensity
+// on the whole colour, mirror part included).
+__global__ void __launch_bounds__(kBlock) k_shade_classic(const JobDesc* __restrict__ jobs, int depth, RayQueue in,
+                                                          const Hit* __restrict__ hits, RayQueue out, ShadowQueue sh,
+                                                          float4* __restrict__ L,
+                                                          unsigned long long* __restrict__ job_counts) {
+    const uint32_t n = *in.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t i = base + lane_id();
+        bool mine = false, emit_shadow = false, emit_child = false;
+        uint32_t jidx = 0, counted = 0;
+        float4 sh_o, sh_d, sh_c, c_o, c_d, c_T;
+        if (i < n) {
+            const float4 d4 = in.d[i];
+            jidx = __float_as_uint(d4.w);
+            mine = jobs[jidx].renderer != kRendererPath;
+            if (mine) {
+                const JobDesc& job = jobs[jidx];
+                const Hit h = hits[i];
+                const float4 o4 = in.o[i];
+                const float4 T = in.T[i];
+                const uint32_t path = __float_as_uint(o4.w);
+                const float4 bg = make_float4(job.bg[0], job.bg[1], job.bg[2], 1.f);
+                if (job.renderer == kRendererRaycast) {
+                    if (h.id >= kMiss) {
+                        L[path] = add4(L[path], mul4(T, bg));
+                    } else {
+                        counted = 1;
+                        const float4* rec = job.sc.shade + 4 * size_t(h.id);
+                        const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2);
+                        const float a = 1.f - (h.r / job.max_visibility);
+                        const float alpha = a < 0.f ? 0.f : (a > 1.f ? 1.f : a);
+                        L[path] = add4(L[path], mul4(T, make_float4(s0.w, s1.w, s2.w, alpha)));
+                    }
+                } else {
+                    counted = 1;
+                    if (h.id >= kMiss) {
+                        L[path] = add4(L[path], mul4(T, bg));
+                    } else {
+                        const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
+                        const float4* rec = job.sc.shade + 4 * size_t(h.id);
+                        const float4 s0 = __ldg(rec), s1 = __ldg(rec + 1), s2 = __ldg(rec + 2), s3 = __ldg(rec + 3);
+                        const float4 diffuse = make_float4(s0.w, s1.w, s2.w, s3.x);
+                        const float rho = s3.y;
+                        const float3 nrm = shading_normal(s0, s1, s2, h);
+                        const float lx = job.light_pos[0] - p.x, ly = job.light_pos[1] - p.y,
+                                    lz = job.light_pos[2] - p.z;
+                        const float inv_l = 1 / sqrtf(lx * lx + ly * ly + lz * lz);
+                        const float cos_a =
+                            fmaxf(0.f, inv_l * lx * nrm.x + inv_l * ly * nrm.y + inv_l * lz * nrm.z);
+                        const float4 direct = mul4(scale4(cos_a, diffuse), make_float4(job.light_col[0],
+                                                                                       job.light_col[1],
+                                                                                       job.light_col[2],
+                                                                                       job.light_col[3]));
+                        const float3 p2 =
+                            make_float3(p.x + nrm.x * 0.0001f, p.y + nrm.y * 0.0001f, p.z + nrm.z * 0.0001f);
+                        float4 f = direct;
+                        if (rho > 0.f) {
+                            f = scale4(1.f - rho, direct);
+                            if (depth < job.max_depth) {
+                                const float4 rc = job.sc.refl ? __ldg(job.sc.refl + h.id)
+                                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+                                const float dn = 2.f * (nrm.x * d4.x + nrm.y * d4.y + nrm.z * d4.z);
+                                c_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
+                                c_d = make_float4(d4.x - dn * nrm.x, d4.y - dn * nrm.y, d4.z - dn * nrm.z,
+                                                  __uint_as_float(jidx));
+                                c_T = mul4(T, scale4(rho, rc));
+                                emit_child = true;
+                            } else {
+                                counted = 2;   // trace(depth + 1) is called and returns 0
+                            }
+                        }
+                        const float qx = job.light_pos[0] - p2.x, qy = job.light_pos[1] - p2.y,
+                                    qz = job.light_pos[2] - p2.z;
+                        const float dist = sqrtf(qx * qx + qy * qy + qz * qz);
+                        const float inv_q = 1 / dist;
+                        sh_o = make_float4(p2.x, p2.y, p2.z, __uint_as_float(path));
+                        // blocked iff some hit has r < dist: the any-hit test keeps r <= tmax
+                        sh_d = make_float4(inv_q * qx, inv_q * qy, inv_q * qz, nextafterf(dist, 0.f));
+                        sh_c = mul4(T, f);
+                        emit_shadow = true;
+                    }
+                }
+            }
+        }
+        if (job_counts) {
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, mine ? jidx : 0xFFFFFFFFu);
+            const unsigned one = __ballot_sync(0xFFFFFFFFu, counted >= 1) & peers;
+            const unsigned two = __ballot_sync(0xFFFFFFFFu, counted == 2) & peers;
+            const unsigned shadow_peers = __ballot_sync(0xFFFFFFFFu, emit_shadow) & peers;
+            if (mine && static_cast<int>(lane_id()) == __ffs(peers) - 1) {
+                const unsigned c = __popc(one) + __popc(two);
+                if (c) atomicAdd(job_counts + 2 * jidx, static_cast<unsigned long long>(c));
+                if (shadow_peers) atomicAdd(job_counts + 2 * jidx + 1, static_cast<unsigned long long>(__popc(shadow_peers)));
+            }
+        }
+        const uint32_t ci = warp_append(out.count, emit_child);
+        if (emit_child) {
+            out.o[ci] = c_o;
+            out.d[ci] = c_d;
+            out.T[ci] = c_T;
+            out.rng[ci] = make_uint2(1u, 0u);
+            if (out.rec) out.rec[ci] = kNoRecord;
+        }
+        const uint32_t si = warp_append(sh.count, emit_shadow);
+        if (emit_shadow) {
+            sh.o[si] = sh_o;
+            sh.d[si] = sh_d;
+            sh.c[si] = sh_c;
+            sh.job[si] = jidx;
+            sh.aux[si] = emit_child ? ci : kAuxNoChild;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- persistent
 // Ray sources for the persistent traversal kernel: where rays come from, which
 // scene they are traced in, and where the answer goes.
@@ -455,6 +588,9 @@ struct ShadowSrc {          // any hit of a shadow queue -> direct light if unbl
     const uint32_t* cnt;
     float4* L;
     bool atomic_l;          // -m > 1 in the batch: several shadow rays of one path per level
+    const uint32_t* aux;    // raytracer jobs in the batch (see ShadowQueue::aux), else null
+    const JobDesc* table;
+    float4* next_T;
     __device__ uint32_t count() const { return *cnt; }
     __device__ void load(uint32_t i, float3& o3, float3& d3, float& tmax, uint32_t& job) const {
         const float4 a = o[i], b = d[i];
@@ -463,15 +599,27 @@ struct ShadowSrc {          // any hit of a shadow queue -> direct light if unbl
         tmax = b.w;
         job = jobs[i];
     }
+    __device__ void add(uint32_t path, float4 ci) const {
+        if (atomic_l) {
+            atomic_add4(L + path, ci);
+        } else {
+            const float4 l = L[path];
+            L[path] = make_float4(l.x + ci.x, l.y + ci.y, l.z + ci.z, l.w + ci.w);
+        }
+    }
     __device__ void store(uint32_t i, const Hit& h) const {
         if (h.id >= kMiss) {
-            const uint32_t path = __float_as_uint(o[i].w);
+            add(__float_as_uint(o[i].w), c[i]);
+        } else if (aux) {
+            const uint32_t a = aux[i];
+            if (a == kAuxPath) return;
+            // a raytracer hit in shadow: color -= color * shadow_intensity
+            const float si = table[jobs[i]].shadow_intensity;
             const float4 ci = c[i];
-            if (atomic_l) {
-                atomic_add4(L + path, ci);
-            } else {
-                const float4 l = L[path];
-                L[path] = make_float4(l.x + ci.x, l.y + ci.y, l.z + ci.z, l.w + ci.w);
+            add(__float_as_uint(o[i].w), sub4(ci, scale4(si, ci)));
+            if (a != kAuxNoChild) {
+                const float4 t = next_T[a];
+                next_T[a] = sub4(t, scale4(si, t));
             }
         }
     }
@@ -699,18 +847,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_flat(SceneView single, const J
 }
 
 __global__ void __launch_bounds__(kBlock) k_shadow_flat(SceneView single, const JobDesc* __restrict__ jobs, bool multi,
-                                                        ShadowQueue sh, float4* __restrict__ L, bool atomic_l) {
-    const uint32_t n = *sh.count;
+                                                        ShadowSrc src) {
+    const uint32_t n = src.count();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = sh.o[i];
-        const float4 d = sh.d[i];
-        const SceneView& sc = multi ? jobs[sh.job[i]].sc : single;
-        const Hit h = traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w);
-        if (h.id >= kMiss) {
-            const uint32_t path = __float_as_uint(o.w);
-            if (atomic_l) atomic_add4(L + path, sh.c[i]);
-            else L[path] = add4(L[path], sh.c[i]);
-        }
+        const float4 o = src.o[i];
+        const float4 d = src.d[i];
+        const SceneView& sc = multi ? jobs[src.jobs[i]].sc : single;
+        src.store(i, traverse<true, false>(sc, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), d.w));
     }
 }
 
@@ -754,8 +897,15 @@ void launch_trace(const SceneView* single, const JobDesc* jobs, const RayQueue& 
 
 void launch_shade(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
                   const ShadowQueue& sh, float4* L, unsigned long long* job_counts, const GuideQueue& gq,
-                  const Records& recs, uint32_t capacity, cudaStream_t stream) {
-    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts, gq, recs);
+                  const Records& recs, uint32_t capacity, bool mixed, cudaStream_t stream) {
+    k_shade<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts, gq, recs,
+                                                       mixed);
+}
+
+void launch_shade_classic(const JobDesc* jobs, int depth, const RayQueue& in, const Hit* hits, const RayQueue& out,
+                          const ShadowQueue& sh, float4* L, unsigned long long* job_counts, uint32_t capacity,
+                          cudaStream_t stream) {
+    k_shade_classic<<<grid_for(capacity), kBlock, 0, stream>>>(jobs, depth, in, hits, out, sh, L, job_counts);
 }
 
 void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, const Hit* hits, float* feat,
@@ -764,15 +914,15 @@ void launch_guide_features(const JobDesc* jobs, int depth, const RayQueue& q, co
 }
 
 void launch_shadow(const SceneView* single, const JobDesc* jobs, const ShadowQueue& sh, float4* L, uint32_t capacity,
-                   bool atomic_l, const TraverseCfg& cfg, cudaStream_t stream) {
+                   bool atomic_l, float4* next_T, const TraverseCfg& cfg, cudaStream_t stream) {
     const SceneView sv = single ? *single : SceneView{};
+    const ShadowSrc src{sh.o, sh.d, sh.c, sh.job, sh.count, L, atomic_l, sh.aux, jobs, next_T};
     if (cfg.persistent) {
-        const ShadowSrc src{sh.o, sh.d, sh.c, sh.job, sh.count, L, atomic_l};
         if (single) run_traverse<ShadowSrc, true, false, false>(sv, jobs, src, capacity, cfg, stream);
         else run_traverse<ShadowSrc, true, false, true>(sv, jobs, src, capacity, cfg, stream);
         return;
     }
-    k_shadow_flat<<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, sh, L, atomic_l);
+    k_shadow_flat<<<grid_for(capacity), kBlock, 0, stream>>>(sv, jobs, single == nullptr, src);
 }
 
 void launch_resolve(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const float4* L, cudaStream_t stream) {
