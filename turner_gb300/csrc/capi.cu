@@ -8,7 +8,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <memory>
+#include <thread>
 #include <mutex>
 #include <new>
 #include <string>
@@ -42,6 +44,30 @@ struct DevBuf {
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host memory, grown on demand: uploads stage through it so that
+// their copies run asynchronously at full link speed.
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~PinnedBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMallocHost(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+};
+
 struct SceneStore {
     bool live = false;
     DevBuf nodes, tri, shade, refl;
@@ -61,6 +87,7 @@ struct turner_ctx {
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
     // render workspace
+    PinnedBuf staging;                 // upload staging (scene records)
     DevBuf L, qa[4], qb[4], hits, shq[3], shjob, shaux, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
     uint64_t acc_key[6] = {};          // what the FP64 running sum belongs to
     uint64_t acc_samples = 0, acc_passes = 0;
@@ -138,54 +165,39 @@ void collect_kernel_times(turner_ctx* ctx) {
     ctx->ev_used.clear();
 }
 
-// Walks the tree from the root as the traversal does and checks that it stays
-// inside the arrays: child indices point forward and in range, leaf ids are
-// valid triangles, every leaf run ends (half-empty leaf or inner node) before
-// the end of the array. Returns the stack depth traversal needs (the largest
-// number of inner nodes on a root-to-leaf path), or -1.
+// Checks that traversal stays inside the arrays: child indices point forward
+// and in range, leaf ids are valid triangles, every leaf run ends (half-empty
+// leaf or inner node) before the end of the array. Returns the stack depth
+// traversal needs (the largest number of inner nodes on a root-to-leaf path),
+// or -1. Every edge of the flattened tree points forward (left child i + 1,
+// right child > i, next leaf of a run i + 1), so one forward pass that only
+// looks at nodes reached from the root visits them after all their parents.
 long validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris) {
     if (n_nodes == 0) return -1;
-    std::vector<uint32_t> order;        // reachable inner nodes, discovery order
-    std::vector<uint8_t> seen(n_nodes, 0);
-    std::vector<uint32_t> st{0};
-    seen[0] = 1;
-    while (!st.empty()) {
-        const uint32_t i = st.back();
-        st.pop_back();
+    std::vector<uint32_t> depth(n_nodes, 0);    // inner nodes above, +1 (0: not reached)
+    depth[0] = 1;
+    uint32_t height = 0;
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        const uint32_t di = depth[i];
+        if (di == 0) continue;
         const uint64_t w = nodes[i];
         const uint32_t lo = static_cast<uint32_t>(w);
         if ((lo & 3u) != 3u) {
             const uint32_t right = lo >> 2;
             if (i + 1 >= n_nodes || right <= i || right >= n_nodes) return -1;
-            order.push_back(i);
-            for (uint32_t c : {i + 1, right}) {
-                if (!seen[c]) {
-                    seen[c] = 1;
-                    st.push_back(c);
-                }
-            }
+            const uint32_t dc = std::min<uint32_t>(di + 1, 1u << 30);
+            depth[i + 1] = std::max(depth[i + 1], dc);
+            depth[right] = std::max(depth[right], dc);
+            height = std::max(height, di);
         } else {
-            for (uint32_t j = i;;) {
-                const uint64_t lw = nodes[j];
-                const uint32_t l = static_cast<uint32_t>(lw);
-                if (static_cast<uint32_t>(lw >> 32) >= n_tris) return -1;
-                if (l == 0xFFFFFFFFu) break;
-                if ((l >> 2) >= n_tris) return -1;
-                if (++j >= n_nodes) return -1;
-                if ((static_cast<uint32_t>(nodes[j]) & 3u) != 3u) break;
-            }
+            if (static_cast<uint32_t>(w >> 32) >= n_tris) return -1;
+            if (lo == 0xFFFFFFFFu) continue;         // half-empty leaf: the run ends
+            if ((lo >> 2) >= n_tris) return -1;
+            if (i + 1 >= n_nodes) return -1;
+            if ((static_cast<uint32_t>(nodes[i + 1]) & 3u) == 3u) depth[i + 1] = std::max(depth[i + 1], di);
         }
     }
-    // depth by decreasing index: children have larger indices than parents
-    std::vector<uint16_t> h(n_nodes, 0);
-    std::sort(order.begin(), order.end());
-    for (auto it = order.rbegin(); it != order.rend(); ++it) {
-        const uint32_t i = *it;
-        const uint32_t right = static_cast<uint32_t>(nodes[i]) >> 2;
-        const uint32_t hl = seen[i + 1] ? h[i + 1] : 0, hr = seen[right] ? h[right] : 0;
-        h[i] = static_cast<uint16_t>(std::min<uint32_t>(60000, 1 + std::max(hl, hr)));
-    }
-    return h[0];
+    return static_cast<long>(height);
 }
 
 void fill_job(const turner_job& j, const SceneView& sc, JobDesc& d) {
@@ -337,42 +349,69 @@ int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes
                         uint32_t n_tris, const float box[6], uint32_t* scene_id) {
     if (!ctx || !nodes || !tris || !box || !scene_id || n_nodes == 0 || n_tris == 0) return TURNER_ERR_INVALID_ARG;
     if (n_tris >= TURNER_MISS || n_nodes >= TURNER_MISS) return TURNER_ERR_TOO_LARGE;
-    const long depth = validate_nodes(nodes, n_nodes, n_tris);
-    if (depth < 0) return TURNER_ERR_BAD_SCENE;
-    if (depth > kStackCap) return TURNER_ERR_TOO_LARGE;
     TURNER_CK(cudaSetDevice(ctx->device));
+    // the node check runs on its own thread while the records are converted
+    auto checked = std::async(std::launch::async, [=]() { return validate_nodes(nodes, n_nodes, n_tris); });
+    auto fail = [&](int status) {
+        checked.wait();
+        return status;
+    };
 
     auto sc = std::unique_ptr<SceneStore>(new (std::nothrow) SceneStore);
-    if (!sc) return TURNER_ERR_OUT_OF_MEMORY;
-    std::vector<float4> tri(4 * size_t(n_tris)), shade(4 * size_t(n_tris)), refl;
+    if (!sc) return fail(TURNER_ERR_OUT_OF_MEMORY);
     bool any_reflective = false;
     for (uint32_t i = 0; i < n_tris && !any_reflective; ++i) any_reflective = tris[i].reflectivity > 0.f;
-    if (any_reflective) refl.resize(n_tris);
-    for (uint32_t i = 0; i < n_tris; ++i) {
-        const turner_triangle& t = tris[i];
-        tri[4 * i + 0] = make_float4(t.vertices[0][0], t.vertices[0][1], t.vertices[0][2], t.uv);
-        tri[4 * i + 1] = make_float4(t.normal[0], t.normal[1], t.normal[2], t.vv);
-        tri[4 * i + 2] = make_float4(t.u[0], t.u[1], t.u[2], t.uu);
-        tri[4 * i + 3] = make_float4(t.v[0], t.v[1], t.v[2], t.denom);
-        shade[4 * i + 0] = make_float4(t.normals[0][0], t.normals[0][1], t.normals[0][2], t.diffuse[0]);
-        shade[4 * i + 1] = make_float4(t.normals[1][0], t.normals[1][1], t.normals[1][2], t.diffuse[1]);
-        shade[4 * i + 2] = make_float4(t.normals[2][0], t.normals[2][1], t.normals[2][2], t.diffuse[2]);
-        shade[4 * i + 3] = make_float4(t.diffuse[3], t.reflectivity, 0.f, 0.f);
-        if (any_reflective) refl[i] = make_float4(t.reflective[0], t.reflective[1], t.reflective[2], t.reflective[3]);
+    // staging layout: node words | intersection records | shading records | reflective colours
+    const size_t node_bytes = sizeof(uint64_t) * n_nodes, rec_bytes = sizeof(float4) * 4 * size_t(n_tris);
+    const size_t refl_bytes = any_reflective ? sizeof(float4) * size_t(n_tris) : 0;
+    const size_t off_tri = (node_bytes + 255) & ~size_t(255), off_shade = off_tri + rec_bytes,
+                 off_refl = off_shade + rec_bytes;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);   // the staging buffer may still feed a copy
+    if (e == cudaSuccess) e = ctx->staging.ensure(off_refl + refl_bytes);
+    if (e != cudaSuccess) return fail(map_cuda(e));
+    char* stage = static_cast<char*>(ctx->staging.p);
+    float4* tri = reinterpret_cast<float4*>(stage + off_tri);
+    float4* shade = reinterpret_cast<float4*>(stage + off_shade);
+    float4* refl = reinterpret_cast<float4*>(stage + off_refl);
+    auto convert = [&](uint32_t b, uint32_t e2) {
+        for (uint32_t i = b; i < e2; ++i) {
+            const turner_triangle& t = tris[i];
+            tri[4 * size_t(i) + 0] = make_float4(t.vertices[0][0], t.vertices[0][1], t.vertices[0][2], t.uv);
+            tri[4 * size_t(i) + 1] = make_float4(t.normal[0], t.normal[1], t.normal[2], t.vv);
+            tri[4 * size_t(i) + 2] = make_float4(t.u[0], t.u[1], t.u[2], t.uu);
+            tri[4 * size_t(i) + 3] = make_float4(t.v[0], t.v[1], t.v[2], t.denom);
+            shade[4 * size_t(i) + 0] = make_float4(t.normals[0][0], t.normals[0][1], t.normals[0][2], t.diffuse[0]);
+            shade[4 * size_t(i) + 1] = make_float4(t.normals[1][0], t.normals[1][1], t.normals[1][2], t.diffuse[1]);
+            shade[4 * size_t(i) + 2] = make_float4(t.normals[2][0], t.normals[2][1], t.normals[2][2], t.diffuse[2]);
+            shade[4 * size_t(i) + 3] = make_float4(t.diffuse[3], t.reflectivity, 0.f, 0.f);
+            if (any_reflective)
+                refl[i] = make_float4(t.reflective[0], t.reflective[1], t.reflective[2], t.reflective[3]);
+        }
+    };
+    {
+        const unsigned hw = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+        const uint32_t per = std::max<uint32_t>(16384, (n_tris + hw - 1) / hw);
+        std::vector<std::thread> pool;
+        for (uint32_t b = per; b < n_tris; b += per) pool.emplace_back(convert, b, std::min(n_tris, b + per));
+        std::memcpy(stage, nodes, node_bytes);
+        convert(0, std::min(n_tris, per));
+        for (auto& th : pool) th.join();
     }
-    TURNER_CK(sc->nodes.ensure(sizeof(uint64_t) * n_nodes));
-    TURNER_CK(sc->tri.ensure(sizeof(float4) * tri.size()));
-    TURNER_CK(sc->shade.ensure(sizeof(float4) * shade.size()));
-    TURNER_CK(cudaMemcpyAsync(sc->nodes.p, nodes, sizeof(uint64_t) * n_nodes, cudaMemcpyHostToDevice, ctx->stream));
-    TURNER_CK(cudaMemcpyAsync(sc->tri.p, tri.data(), sizeof(float4) * tri.size(), cudaMemcpyHostToDevice, ctx->stream));
-    TURNER_CK(cudaMemcpyAsync(sc->shade.p, shade.data(), sizeof(float4) * shade.size(), cudaMemcpyHostToDevice,
-                              ctx->stream));
-    if (any_reflective) {
-        TURNER_CK(sc->refl.ensure(sizeof(float4) * refl.size()));
-        TURNER_CK(cudaMemcpyAsync(sc->refl.p, refl.data(), sizeof(float4) * refl.size(), cudaMemcpyHostToDevice,
-                                  ctx->stream));
-    }
-    TURNER_CK(cudaStreamSynchronize(ctx->stream));
+    e = sc->nodes.ensure(node_bytes);
+    if (e == cudaSuccess) e = sc->tri.ensure(rec_bytes);
+    if (e == cudaSuccess) e = sc->shade.ensure(rec_bytes);
+    if (e == cudaSuccess && any_reflective) e = sc->refl.ensure(refl_bytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sc->nodes.p, stage, node_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sc->tri.p, tri, rec_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sc->shade.p, shade, rec_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && any_reflective)
+        e = cudaMemcpyAsync(sc->refl.p, refl, refl_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    const long depth = checked.get();
+    const cudaError_t es = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = es;
+    if (e != cudaSuccess) return map_cuda(e);
+    if (depth < 0) return TURNER_ERR_BAD_SCENE;
+    if (depth > kStackCap) return TURNER_ERR_TOO_LARGE;
     SceneView& v = sc->view;
     v.nodes = sc->nodes.as<uint2>();
     v.tri = sc->tri.as<float4>();
