@@ -383,6 +383,20 @@ void turner_kdtree_free(turner_kdtree* tree);
  * Whitted raytracer reads (raytracer.cpp:46-55). They do not change the tree. */
 int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective);
 
+/* Builds a kd-tree on the context's GPU, level by level: SAH with the
+ * reference's cost constants and termination test over 32 bins per axis in
+ * large cells and over every box bound in cells of at most 64 triangles,
+ * triangles classified by their bounding boxes clipped to each cell. No counterpart
+ * for the build itself: the reference builds on the host
+ * (lib/kdtree.cpp:124-412), and its node words depend on std::sort's order
+ * among equal events, so this tree is not the reference's. It is in the same
+ * FlatNode format with the same triangle records, and every leaf lists every
+ * triangle whose box meets its cell, so closest hits agree with the
+ * reference's tree except where the reference's own thick-plane clipping
+ * leaves a triangle out. Synchronous; allocates device memory while it runs. */
+int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float* normals, const float* diffuse,
+                            uint32_t n_tris, turner_kdtree** out);
+
 /* ---------------------------------------------------------- tree files */
 /* A binary file holding one kd-tree (node words, triangle records, box),
  * keyed by the content of the triangles it was built from. Replaces the

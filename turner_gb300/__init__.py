@@ -150,6 +150,7 @@ def _lib() -> C.CDLL:
         "turner_upload_kdtree": (C.c_int, [_P, _P, C.POINTER(C.c_uint32)]),
         "turner_kdtree_free": (None, [_P]),
         "turner_mesh_key": (C.c_uint64, [_P, _P, _P, C.c_uint32]),
+        "turner_kdtree_build_gpu": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.POINTER(_P)]),
         "turner_kdtree_save": (C.c_int, [_P, C.c_uint64, C.c_char_p]),
         "turner_kdtree_load": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(_P)]),
         "turner_kdtree_build_cached": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, C.c_char_p, C.POINTER(_P),
@@ -282,6 +283,20 @@ class KDTree:
         if r.shape[0] != self.num_triangles():
             raise ValueError("one row per triangle")
         _check(_lib().turner_kdtree_set_reflective(self._h, _ptr(r)), "turner_kdtree_set_reflective")
+
+    @classmethod
+    def build_gpu(cls, ctx: "Context", mesh: Mesh) -> "KDTree":
+        """Binned-SAH kd-tree built on the context's GPU (same FlatNode format
+        and triangle records; not the reference's node words)."""
+        v, nr, d = _mesh_arrays(mesh.vertices, mesh.normals, mesh.diffuse)
+        t = cls.__new__(cls)
+        t._h = _P()
+        _check(_lib().turner_kdtree_build_gpu(ctx._h, _ptr(v), _ptr(nr), _ptr(d), v.shape[0], C.byref(t._h)),
+               "turner_kdtree_build_gpu")
+        t.from_cache = False
+        if mesh.reflective is not None:
+            t.set_reflective(mesh.reflective)
+        return t
 
     @classmethod
     def load(cls, path, key: int = 0) -> "KDTree":

@@ -34,6 +34,7 @@ CUDA_UNITS = [
     (CSRC / "trace_kernels.cu", ["-fmad=false"]),
     (CSRC / "capi.cu", []),
     (CSRC / "guide.cu", []),
+    (CSRC / "kdtree_gpu.cu", []),
 ]
 HOST_UNITS = [
     CSRC / "host" / "scenes.cpp",

@@ -417,6 +417,50 @@ Box triangle_box(const turner_triangle& t) {
 
 } // namespace
 
+namespace turner {
+namespace host {
+
+Box records_and_box(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris,
+                    std::vector<turner_triangle>& tris) {
+    tris.resize(n_tris);
+    for (uint32_t i = 0; i < n_tris; ++i) {
+        turner_triangle& t = tris[i];
+        std::memset(&t, 0, sizeof(t));
+        std::memcpy(t.vertices, vertices + 9 * size_t(i), 9 * sizeof(float));
+        if (normals) std::memcpy(t.normals, normals + 9 * size_t(i), 9 * sizeof(float));
+        if (diffuse) {
+            std::memcpy(t.diffuse, diffuse + 4 * size_t(i), 4 * sizeof(float));
+            // main.cpp:43 reads the emissive colour from the diffuse key
+            std::memcpy(t.emissive, diffuse + 4 * size_t(i), 4 * sizeof(float));
+        }
+        precompute(t);
+    }
+    // KDTree::KDTree (lib/kdtree.cpp:474-490): box = union of triangle boxes
+    Box box = triangle_box(tris[0]);
+    for (uint32_t i = 1; i < n_tris; ++i) {
+        const Box b = triangle_box(tris[i]);
+        P3 lo, hi;
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(box.lo[k], b.lo[k]);
+            hi[k] = std::max(box.hi[k], b.hi[k]);
+        }
+        box = make_box(lo, hi);
+    }
+    return box;
+}
+
+void make_records(const float* vertices, const float* normals, const float* diffuse, uint32_t n_tris,
+                  std::vector<turner_triangle>& tris, float box[6]) {
+    const Box b = records_and_box(vertices, normals, diffuse, n_tris, tris);
+    for (int k = 0; k < 3; ++k) {
+        box[k] = b.lo[k];
+        box[3 + k] = b.hi[k];
+    }
+}
+
+} // namespace host
+} // namespace turner
+
 extern "C" {
 
 int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective) {
@@ -435,32 +479,9 @@ int turner_kdtree_build(const float* vertices, const float* normals, const float
     auto tree = std::unique_ptr<turner_kdtree>(new (std::nothrow) turner_kdtree);
     if (!tree) return TURNER_ERR_OUT_OF_MEMORY;
     try {
-        tree->tris.resize(n_tris);
-        for (uint32_t i = 0; i < n_tris; ++i) {
-            turner_triangle& t = tree->tris[i];
-            std::memset(&t, 0, sizeof(t));
-            std::memcpy(t.vertices, vertices + 9 * size_t(i), 9 * sizeof(float));
-            if (normals) std::memcpy(t.normals, normals + 9 * size_t(i), 9 * sizeof(float));
-            if (diffuse) {
-                std::memcpy(t.diffuse, diffuse + 4 * size_t(i), 4 * sizeof(float));
-                // main.cpp:43 reads the emissive colour from the diffuse key
-                std::memcpy(t.emissive, diffuse + 4 * size_t(i), 4 * sizeof(float));
-            }
-            precompute(t);
-        }
-        // KDTree::KDTree (lib/kdtree.cpp:474-490): box = union of triangle boxes
-        Box box = triangle_box(tree->tris[0]);
+        const Box box = turner::host::records_and_box(vertices, normals, diffuse, n_tris, tree->tris);
         std::vector<uint32_t> ids(n_tris);
         for (uint32_t i = 0; i < n_tris; ++i) ids[i] = i;
-        for (uint32_t i = 1; i < n_tris; ++i) {
-            const Box b = triangle_box(tree->tris[i]);
-            P3 lo, hi;
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = std::min(box.lo[k], b.lo[k]);
-                hi[k] = std::max(box.hi[k], b.hi[k]);
-            }
-            box = make_box(lo, hi);
-        }
         if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
         int par_depth = 0;
         while ((1 << par_depth) < 2 * threads && par_depth < 12) ++par_depth;
