@@ -278,8 +278,9 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
  *                  (exact: a repeat cannot change the answer; 128-thread blocks)
  *   min_blocks     10, 12 or 16: cap traversal registers so that many 128-thread
  *                  blocks fit per SM (48, 40, 32 registers), 0: no cap.
- *                  Default 12: the traversal is latency-bound and 12 blocks
- *                  beat the uncapped 9 despite a few spilled registers */
+ *                  Default 10: the traversal is latency-bound and 10 blocks
+ *                  beat the uncapped 9 (56 registers) and the 12 at 40
+ *                  registers, which spill more */
 typedef struct turner_tuning {
     int32_t persistent;
     uint32_t blocks_per_sm;

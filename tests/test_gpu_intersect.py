@@ -149,6 +149,31 @@ def test_edge_rays(ctx, uploaded):
     assert np.array_equal(gpu[0], cpu[0])
 
 
+@pytest.mark.parametrize("kind,kw", [(tg.SCENE_SPHERE_ROOM, dict(detail=5)), (tg.SCENE_SOUP, dict(count=5000, seed=9))])
+def test_vertex_and_edge_aimed_rays(ctx, kind, kw):
+    """Rays aimed at triangle vertices, edge midpoints and points just inside
+    and outside edges: the barycentric numerators are zero or a few ulps from
+    it, where the sign tests that skip divides must agree with dividing."""
+    mesh = tg.make_scene(kind, **kw)
+    t = tg.KDTree.from_mesh(mesh)
+    nodes, tris, box = t.export()
+    sid, ref = ctx.upload(nodes, tris, box), orc.Scene(nodes, tris, box)
+    rng = np.random.default_rng(31)
+    v = mesh.vertices.reshape(-1, 3, 3).astype(np.float64)
+    pick = rng.integers(0, v.shape[0], 40_000)
+    a, b, c = v[pick, 0], v[pick, 1], v[pick, 2]
+    w = rng.integers(0, 4, pick.size)[:, None]
+    eps = rng.choice([0.0, 1e-7, -1e-7, 1e-6, -1e-6], pick.size)[:, None]
+    mid = 0.5 * (a + b)
+    target = np.where(w == 0, a, np.where(w == 1, mid, np.where(w == 2, mid + eps * (c - mid), (a + b + c) / 3)))
+    lo, hi = np.array(box[:3]), np.array(box[3:])
+    org = lo + (hi - lo) * rng.random((pick.size, 3))
+    d = target - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o32, d32 = org.T.astype(np.float32).copy(), d.T.astype(np.float32).copy()
+    assert_same(ctx.intersect(sid, o32, d32), ref.intersect(o32, d32))
+
+
 def test_device_buffers(ctx, uploaded):
     torch = pytest.importorskip("torch")
     sid, ref, box = uploaded["sphere5"]

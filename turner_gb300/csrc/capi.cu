@@ -1053,7 +1053,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
         return TURNER_OK;
     };
     // coordinate descent from the defaults, one knob at a time
-    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 12, 0, 0};
+    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 10, 0, 0};
     int s = measure(cur, cur.ms);
     if (s != TURNER_OK) return s;
     const uint32_t blocks[] = {128, 256};

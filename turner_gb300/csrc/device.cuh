@@ -65,6 +65,13 @@ __device__ __forceinline__ bool triangle_test(const float4* __restrict__ tri, ui
     return true;
 }
 
+// true only if the IEEE quotient x / y is < 0: the signs differ and |x / y|
+// > 2^-100, so the rounded quotient is a negative normal number, never -0.
+// NaN operands and tiny quotients answer false (the caller divides).
+__device__ __forceinline__ bool quotient_negative(float x, float y) {
+    return ((__float_as_uint(x) ^ __float_as_uint(y)) & 0x80000000u) && fabsf(x) > fabsf(y) * 7.8886090522101181e-31f;
+}
+
 // triangle_test restricted to candidates that can change a traversal's
 // answer: a valid intersection with r < bound (closest hit, bound = best r
 // so far) or r <= bound (any hit, bound = distance to the light). Skipping
@@ -73,8 +80,9 @@ __device__ __forceinline__ bool triangle_test(const float4* __restrict__ tri, ui
 // valid r <= dist exists. NaN r never satisfies either comparison.
 //   - r < 0 is decided from the signs of nom and denom when nom/denom cannot
 //     underflow to -0 (|nom| > |denom| * 2^-100), without dividing;
-//   - s and t (two divides, the second 32-byte half of the record) are only
-//     computed for r inside the bound.
+//   - s and t (the second 32-byte half of the record) are only computed for
+//     r inside the bound, and their two divides only when neither numerator
+//     has the opposite sign of the common denominator.
 template <bool INCLUSIVE>
 __device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__ tri, uint32_t id, float3 o, float3 d,
                                                       float bound, float& r, float& s, float& t) {
@@ -83,10 +91,7 @@ __device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__
     const float denom = n.x * d.x + n.y * d.y + n.z * d.z;
     if (denom == 0.f) return false;
     const float nom = n.x * (a.x - o.x) + n.y * (a.y - o.y) + n.z * (a.z - o.z);
-    if (((__float_as_uint(nom) ^ __float_as_uint(denom)) & 0x80000000u) &&
-        fabsf(nom) > fabsf(denom) * 7.8886090522101181e-31f) {
-        return false;                                    // r < 0
-    }
+    if (quotient_negative(nom, denom)) return false;    // r < 0
     r = nom / denom;
     if (INCLUSIVE ? !(r <= bound) : !(r < bound)) return false;
     if (r < 0) return false;
@@ -97,14 +102,33 @@ __device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__
     const float wz = (o.z + r * d.z) - a.z;
     const float wv = wx * v.x + wy * v.y + wz * v.z;
     const float wu = wx * u.x + wy * u.y + wz * u.z;
-    s = (a.w * wv - n.w * wu) / v.w;
+    const float s_num = a.w * wv - n.w * wu;
+    const float t_num = a.w * wu - u.w * wv;
+    // s < 0 or t < 0 from the signs, as for r above; both divides only for
+    // points that can lie inside the triangle
+    if (quotient_negative(s_num, v.w) || quotient_negative(t_num, v.w)) return false;
+    s = s_num / v.w;
     if (s < 0) return false;
-    t = (a.w * wu - u.w * wv) / v.w;
+    t = t_num / v.w;
     if (t < 0 || 1 < s + t) return false;
     return true;
 }
 
 __device__ __forceinline__ float pick(float3 v, uint32_t ax) { return ax == 0 ? v.x : (ax == 1 ? v.y : v.z); }
+
+// Traversal stacks. An entry is {far child, exit distance of the cell it was
+// split from}; its entry distance is not stored. Between a push and the
+// matching pop the current exit distance is exactly the pushed split
+// distance t (a push sets texit = t, descents without a push leave it, and a
+// pop restores the exit that the entry below it recorded), so a pop takes
+// tenter = texit and texit = the stored exit: the same floats the reference's
+// three-field stack (lib/kdtree.cpp:530-560) holds, in 8 bytes instead of 12.
+template <int N>
+struct LocalStack {
+    uint2 e[N];
+    __device__ __forceinline__ void put(int k, uint2 v) { e[k] = v; }
+    __device__ __forceinline__ uint2 get(int k) const { return e[k]; }
+};
 
 // KDTreeIntersection::intersect (lib/kdtree.cpp:516-607).
 //   CLOSEST: every leaf overlapped by [tenter, texit] is visited in the
@@ -138,8 +162,7 @@ __device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d,
         if (texit < tenter) return best;
     }
 
-    uint32_t st_node[kStackCap];
-    float st_enter[kStackCap], st_exit[kStackCap];
+    LocalStack<kStackCap> st;
     int sp = 0;
     uint32_t node = 0;
     const uint2* __restrict__ nodes = sc.nodes;
@@ -159,9 +182,7 @@ __device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d,
             } else if (t < tenter) {
                 node = far_c;
             } else {
-                st_node[sp] = far_c;
-                st_enter[sp] = t;
-                st_exit[sp] = texit;
+                st.put(sp, make_uint2(far_c, __float_as_uint(texit)));
                 ++sp;
                 node = near_c;
                 texit = t;
@@ -197,11 +218,12 @@ __device__ __forceinline__ Hit traverse(const SceneView& sc, float3 o, float3 d,
             // cells are popped in increasing entry distance along the ray;
             // a hit closer than the next cell's entry (with margin for the
             // thick-plane classification of the builder) cannot be beaten
-            if (best.r < st_enter[sp] - (1e-3f + 1e-3f * fabsf(st_enter[sp]))) break;
+            if (best.r < texit - (1e-3f + 1e-3f * fabsf(texit))) break;
         }
-        node = st_node[sp];
-        tenter = st_enter[sp];
-        texit = st_exit[sp];
+        const uint2 e = st.get(sp);
+        node = e.x;
+        tenter = texit;   // the popped cell starts at the split plane, the current exit
+        texit = __uint_as_float(e.y);
     }
     return best;
 }
@@ -269,9 +291,8 @@ __device__ __forceinline__ bool trav_begin(const SceneView& sc, float3 o, float3
 
 // One round: descend from s.node to a leaf, test its run, pop the next cell.
 // Returns true when the ray is finished (s.best holds the answer).
-template <bool ANY, bool FAST_EXIT, bool MAILBOX = false>
-__device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* st_node, float* st_enter,
-                                           float* st_exit) {
+template <bool ANY, bool FAST_EXIT, bool MAILBOX = false, class Stack>
+__device__ __forceinline__ bool trav_round(TravState& s, float tmax, Stack& st) {
     const uint2* __restrict__ nodes = s.nodes;
     uint32_t node = s.node;
     float tenter = s.tenter, texit = s.texit;
@@ -291,9 +312,7 @@ __device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* s
         } else if (t < tenter) {
             node = far_c;
         } else {
-            st_node[sp] = far_c;
-            st_enter[sp] = t;
-            st_exit[sp] = texit;
+            st.put(sp, make_uint2(far_c, __float_as_uint(texit)));
             ++sp;
             node = near_c;
             texit = t;
@@ -301,13 +320,18 @@ __device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* s
         w = __ldg(nodes + node);
     }
     for (;;) {
+        // a full pair is always followed by another word (a leaf or the
+        // run's sentinel): fetch it while the pair is tested
+        const bool pair = w.x != 0xFFFFFFFFu;
+        uint2 next = w;
+        if (pair) next = __ldg(nodes + node + 1);
         float r, u, v;
         if (!mailbox_seen<MAILBOX>(s, w.y) &&
             triangle_test_bounded<ANY>(s.tri, w.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
             s.best = Hit{w.y, r, u, v};
             if (ANY) return true;
         }
-        if (w.x == 0xFFFFFFFFu) break;
+        if (!pair) break;
         const uint32_t id2 = w.x >> 2;
         if (!mailbox_seen<MAILBOX>(s, id2) &&
             triangle_test_bounded<ANY>(s.tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
@@ -315,17 +339,18 @@ __device__ __forceinline__ bool trav_round(TravState& s, float tmax, uint32_t* s
             if (ANY) return true;
         }
         ++node;
-        w = __ldg(nodes + node);
+        w = next;
         if ((w.x & 3u) != 3u) break;
     }
     if (sp == 0) return true;
     --sp;
     if (FAST_EXIT && !ANY) {
-        if (s.best.r < st_enter[sp] - (1e-3f + 1e-3f * fabsf(st_enter[sp]))) return true;
+        if (s.best.r < texit - (1e-3f + 1e-3f * fabsf(texit))) return true;
     }
-    s.node = st_node[sp];
-    s.tenter = st_enter[sp];
-    s.texit = st_exit[sp];
+    const uint2 e = st.get(sp);
+    s.node = e.x;
+    s.tenter = texit;
+    s.texit = __uint_as_float(e.y);
     s.sp = sp;
     return false;
 }

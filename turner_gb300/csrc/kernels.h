@@ -99,8 +99,8 @@ struct TraverseCfg {
     unsigned block = 128;         // threads per block of the persistent kernels: 128 or 256
     unsigned stack = kStackCap;   // traversal stack entries: 64 or kStackCap (128)
     bool mailbox = false;         // skip repeated tests of a triangle (128-thread blocks)
-    unsigned min_blocks = 12;     // 10, 12, 16: cap registers so that many blocks fit per SM (128-thread
-                                  // blocks); 0: no cap. 12 (40 registers) is fastest on GB300
+    unsigned min_blocks = 10;     // 10, 12, 16: cap registers so that many blocks fit per SM (128-thread
+                                  // blocks); 0: no cap. 10 (48 registers) is fastest on GB300
     uint32_t* work = nullptr;
 };
 

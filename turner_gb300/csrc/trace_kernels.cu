@@ -650,12 +650,10 @@ struct SoaSrc {             // turner_intersect batches
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
 // while rays of very different lengths are traversed. MULTI: every ray names
 // its job and is traced in that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX>
+template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, class Stack>
 __device__ __forceinline__ void traverse_persistent(const SceneView& single, const JobDesc* __restrict__ jobs,
-                                                    Src& src, uint32_t* __restrict__ work) {
+                                                    Src& src, uint32_t* __restrict__ work, Stack& st) {
     const uint32_t n = src.count();
-    uint32_t st_node[STACK];
-    float st_enter[STACK], st_exit[STACK];
     TravState s;
     uint32_t cur = 0;
     bool active = false, exhausted = false;
@@ -688,7 +686,7 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
-        if (active && trav_round<ANY, FAST, MAILBOX>(s, tmax, st_node, st_enter, st_exit)) {
+        if (active && trav_round<ANY, FAST, MAILBOX>(s, tmax, st)) {
             src.store(cur, s.best);
             active = false;
         }
@@ -702,13 +700,15 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX>
 __global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
                                                      uint32_t* __restrict__ work) {
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work);
+    LocalStack<STACK> st;
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, st);
 }
 
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_traverse_capped(SceneView single, const JobDesc* __restrict__ jobs,
                                                                   Src src, uint32_t* __restrict__ work) {
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work);
+    LocalStack<STACK> st;
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, st);
 }
 
 // Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
