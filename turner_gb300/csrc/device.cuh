@@ -83,11 +83,20 @@ __device__ __forceinline__ bool quotient_negative(float x, float y) {
 //   - s and t (the second 32-byte half of the record) are only computed for
 //     r inside the bound, and their two divides only when neither numerator
 //     has the opposite sign of the common denominator.
+// One 32-byte read-only load (sm_100 and later); p must be 32-byte aligned.
+// Intersection records are 64 bytes and the array is 256-byte aligned, so
+// each half of a record is one such load: one L1 request instead of two.
+__device__ __forceinline__ void ldg_pair(const float4* p, float4& x, float4& y) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w), "=f"(y.x), "=f"(y.y), "=f"(y.z), "=f"(y.w)
+        : "l"(p));
+}
+
 template <bool INCLUSIVE>
 __device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__ tri, uint32_t id, float3 o, float3 d,
                                                       float bound, float& r, float& s, float& t) {
-    const float4 a = __ldg(tri + 4 * size_t(id) + 0);   // v0, uv
-    const float4 n = __ldg(tri + 4 * size_t(id) + 1);   // normal, vv
+    float4 a, n;   // {v0, uv}, {normal, vv}
+    ldg_pair(tri + 4 * size_t(id), a, n);
     const float denom = n.x * d.x + n.y * d.y + n.z * d.z;
     if (denom == 0.f) return false;
     const float nom = n.x * (a.x - o.x) + n.y * (a.y - o.y) + n.z * (a.z - o.z);
@@ -95,8 +104,8 @@ __device__ __forceinline__ bool triangle_test_bounded(const float4* __restrict__
     r = nom / denom;
     if (INCLUSIVE ? !(r <= bound) : !(r < bound)) return false;
     if (r < 0) return false;
-    const float4 u = __ldg(tri + 4 * size_t(id) + 2);   // u, uu
-    const float4 v = __ldg(tri + 4 * size_t(id) + 3);   // v, denom
+    float4 u, v;   // {u, uu}, {v, denom}
+    ldg_pair(tri + 4 * size_t(id) + 2, u, v);
     const float wx = (o.x + r * d.x) - a.x;
     const float wy = (o.y + r * d.y) - a.y;
     const float wz = (o.z + r * d.z) - a.z;
