@@ -6,19 +6,30 @@
 // sweeps exact event lists sorted with std::sort, whose order among equal
 // keys is that library's and decides the triangle order inside leaves. This
 // build chooses planes among 32 bins per axis for large cells and among all
-// box bounds for cells of at most 64 references, and clips triangles by their
-// bounding boxes, so its tree differs. Every leaf lists every triangle whose
-// box reaches into the leaf's cell, so closest hits are the same triangles at
-// the same r (checked against a brute-force leaf and the reference's tree in
-// the tests).
+// clipped-box bounds for cells of at most kExactMax references, so its tree
+// differs. Every leaf lists every triangle whose clipped box reaches into the
+// leaf's cell, so closest hits are the same triangles at the same r (checked
+// against a brute-force leaf and the reference's tree in the tests).
+//
+// Splits leave triangles on both sides. The flattening drops an empty child
+// (so does the reference's, lib/kdtree.cpp:164-172), and with it the cut: an
+// empty-space split never narrows a cell that the traversal sees, although
+// the SAH credits it with the space it cuts off (and with the 0.8 empty-side
+// factor of lib/kdtree.cpp:182-187). Allowing such splits built thin slab
+// cells around curved surfaces (twice the node visits and triangle tests of
+// the reference's tree on the 327,692-triangle sphere room); without them the
+// same build needs about two thirds of the reference tree's visits and a
+// quarter of its tests. (The reference's own builder seldom cuts empty space:
+// a triangle whose clipped polygon has fewer than two points gets an
+// unbounded box there and sits on both sides of every later plane.)
 //
 // Per level (one CUDA block per node):
 //   k_level     bounding box of each triangle reference clipped to the node's
 //               cell, 32-bin start/end histograms per axis in shared memory
 //               (or, in small cells, the boxes themselves), SAH of the
 //               3 x 31 bin boundaries (or of every box bound) with the reference's
-//               constants (traversal 15, intersection 20, empty-side factor
-//               0.8, lib/kdtree.cpp:178-203) and its termination test, then
+//               constants (traversal 15, intersection 20, lib/kdtree.cpp:178-203)
+//               and its termination test, then
 //               per reference: left / right / leaf flags
 //   scans       exclusive scans of the flags (per reference) and of the
 //               children, next-level references and leaf references (per node)
@@ -48,7 +59,7 @@ constexpr int kScanBlock = kScanThreads * kScanItems;
 constexpr uint32_t kMaxBuildDepth = 60;               // flattened depth, < the traversal stack (128 entries)
 constexpr uint32_t kMaxLevels = 512;                  // breadth-first levels, counting empty-space cuts
 constexpr uint32_t kExactMax = 1024;                  // cells this small sweep every box bound
-constexpr float kCostTraversal = 15.f, kCostIntersection = 20.f, kEmptyFactor = 0.8f;
+constexpr float kCostTraversal = 15.f, kCostIntersection = 20.f;
 
 struct Cell {
     float lo[3], hi[3];
@@ -190,9 +201,8 @@ __device__ __forceinline__ float split_cost(const Cell& c, float sa, int a, floa
     }
     lhi[a] = pos;
     rlo[a] = pos;
-    const float lam = (nl == 0 || nr == 0) ? kEmptyFactor : 1.f;
-    return lam * (kCostTraversal + kCostIntersection * (surface(llo, lhi) / sa * static_cast<float>(nl) +
-                                                       surface(rlo, rhi) / sa * static_cast<float>(nr)));
+    return kCostTraversal + kCostIntersection * (surface(llo, lhi) / sa * static_cast<float>(nl) +
+                                                 surface(rlo, rhi) / sa * static_cast<float>(nr));
 }
 
 // Which side of the plane a clipped box goes to: left if it starts before the
@@ -218,11 +228,11 @@ __device__ __forceinline__ void consider(const Cell& c, float sa, uint32_t n, in
     for (int pl = 1; pl >= 0; --pl) {
         const uint32_t l = nl + (pl ? np : 0u), r = nr + (pl ? 0u : np);
         if (l == n && r == n) continue;   // separates nothing
-        if (l == 0 && r == 0) continue;
+        if (l == 0 || r == 0) continue;   // empty space: the flattening would drop the cut
         // a plane in a face is useful only to move the boxes lying in it
-        // into a flat cell: not to leave that cell empty or the cell whole
-        if (pos == c.lo[a] && (l == 0 || r == n)) continue;
-        if (pos == c.hi[a] && (r == 0 || l == n)) continue;
+        // into a flat cell, not to keep the cell whole
+        if (pos == c.lo[a] && r == n) continue;
+        if (pos == c.hi[a] && l == n) continue;
         const float cost = split_cost(c, sa, a, pos, l, r);
         if (better(cost, a, pos, pl, bc, ba, bp, bpl)) {
             bc = cost;
@@ -361,9 +371,9 @@ __global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict_
         Decision r{0, 0, 0.f, n, 1};
         if (n > 3 && c.depth < kMaxBuildDepth && !last_level && r_axis[0] < 3) {
             // the termination test of lib/kdtree.cpp:151-159: a leaf when
-            // intersecting everything costs less than the best split
-            const float lam = (r_nl[0] == 0 || r_nr[0] == 0) ? kEmptyFactor : 1.f;
-            if (!(kCostIntersection * static_cast<float>(n) * lam < r_cost[0])) {
+            // intersecting everything costs less than the best split (both
+            // sides are non-empty, so its empty-side factor is 1)
+            if (!(kCostIntersection * static_cast<float>(n) < r_cost[0])) {
                 r.split = 1;
                 r.axis = r_axis[0];
                 r.pos = r_pos[0];
