@@ -95,6 +95,22 @@ def test_gpu_tree_renders_like_the_reference_tree(ctx):
     assert abs(int(sa.rays) - int(sb.rays)) <= 0.005 * int(sb.rays)
 
 
+@pytest.mark.parametrize("name,visits,tests", [("sphere5", 0.75, 0.4), ("soup3000", 1.05, 0.6)])
+def test_gpu_tree_quality(ctx, name, visits, tests):
+    """Traversal work on the GPU-built tree against the reference's tree, as
+    the oracle counts it on the same rays (node visits, triangle tests). An
+    empty-space split, which the flattening drops, once made slab-shaped
+    cells with twice the reference tree's work on curved surfaces."""
+    m = tg.make_scene(**SCENES[name])
+    o, d = tg.make_rays(20_000, tg.KDTree.from_mesh(m).export()[2], seed=5)
+    counts = {}
+    for label, t in (("gpu", tg.KDTree.build_gpu(ctx, m)), ("ref", tg.KDTree.from_mesh(m))):
+        nodes, tris, box = t.export()
+        counts[label] = orc.Scene(nodes, tris, box).intersect(o, d, counts=True)[4]
+    assert counts["gpu"][0] <= visits * counts["ref"][0], counts
+    assert counts["gpu"][1] <= tests * counts["ref"][1], counts
+
+
 def test_gpu_build_rejects_bad_input(ctx):
     with pytest.raises(tg.TurnerError):
         tg.KDTree.build_gpu(ctx, tg.Mesh(np.zeros((0, 9), np.float32), np.zeros((0, 9), np.float32),
