@@ -386,8 +386,9 @@ int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective);
 
 /* Builds a kd-tree on the context's GPU, level by level: SAH with the
  * reference's cost constants and termination test over 32 bins per axis in
- * large cells and over every box bound in cells of at most 64 triangles,
- * triangles classified by their bounding boxes clipped to each cell. No counterpart
+ * large cells and over every clipped-box bound in cells of at most 1024
+ * triangles, triangles classified by their polygons clipped to each cell,
+ * and no empty-space splits (the flattened tree could not keep them). No counterpart
  * for the build itself: the reference builds on the host
  * (lib/kdtree.cpp:124-412), and its node words depend on std::sort's order
  * among equal events, so this tree is not the reference's. It is in the same
