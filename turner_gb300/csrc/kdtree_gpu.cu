@@ -59,6 +59,8 @@ constexpr int kScanBlock = kScanThreads * kScanItems;
 constexpr uint32_t kMaxBuildDepth = 60;               // flattened depth, < the traversal stack (128 entries)
 constexpr uint32_t kMaxLevels = 512;                  // breadth-first levels, counting empty-space cuts
 constexpr uint32_t kExactMax = 1024;                  // cells this small sweep every box bound
+constexpr uint32_t kSmallMax = 32;                    // cells this small take one warp instead of a block
+constexpr int kSmallWarps = 8;                        // warps (cells) per block of k_level_small
 constexpr float kCostTraversal = 15.f, kCostIntersection = 20.f;
 
 struct Cell {
@@ -245,14 +247,15 @@ __device__ __forceinline__ void consider(const Cell& c, float sa, uint32_t n, in
     }
 }
 
-// One block per cell: the best split, the decision and the per-reference
-// flags (low 32 bits: goes left / stays in the leaf; high 32 bits: goes
-// right). Cells with at most kExactMax references sweep every clipped-box
+// One block per listed cell (the cells of more than kSmallMax references):
+// the best split, the decision and the per-reference flags (low 32 bits: goes
+// left / stays in the leaf; high 32 bits: goes right). Cells with at most kExactMax references sweep every clipped-box
 // bound as a candidate plane, as the reference's event sweep does; larger
 // cells evaluate 31 bin boundaries per axis from start / end histograms and
 // the two faces of the cell (where boxes lying in a face can be split off
 // into a flat cell, as the reference's planar events allow).
-__global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict__ cells, const uint32_t* __restrict__ refs,
+__global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict__ cells, const uint32_t* __restrict__ list,
+                                                         const uint32_t* __restrict__ refs,
                                                          const float* __restrict__ verts,
                                                          const float* __restrict__ tri_box, bool last_level,
                                                          Decision* __restrict__ dec, uint64_t* __restrict__ flags) {
@@ -264,7 +267,8 @@ __global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict_
     __shared__ int r_axis[kLevelThreads], r_pl[kLevelThreads];
     __shared__ uint32_t r_nl[kLevelThreads], r_nr[kLevelThreads];
     __shared__ Decision d;
-    const Cell c = cells[blockIdx.x];
+    const uint32_t ci = list[blockIdx.x];
+    const Cell c = cells[ci];
     const int tid = threadIdx.x;
     const bool exact = c.count <= kExactMax;
     for (int k = tid; k < 3 * kBins; k += kLevelThreads) {
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict_
             }
         }
         d = r;
-        dec[blockIdx.x] = r;
+        dec[ci] = r;
     }
     __syncthreads();
     for (uint32_t i = tid; i < c.count; i += kLevelThreads) {
@@ -398,6 +402,107 @@ __global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict_
             }
         }
         flags[c.begin + i] = f;
+    }
+}
+
+// One warp per listed cell of at most kSmallMax references (one reference per
+// lane): the same clipping, exact candidate sweep, choice and termination test
+// as k_level, without its block-wide histograms and reductions. Deep levels
+// hold hundreds of thousands of such cells.
+__global__ void __launch_bounds__(32 * kSmallWarps) k_level_small(const Cell* __restrict__ cells,
+                                                                  const uint32_t* __restrict__ list, uint32_t n_list,
+                                                                  const uint32_t* __restrict__ refs,
+                                                                  const float* __restrict__ verts,
+                                                                  const float* __restrict__ tri_box, bool last_level,
+                                                                  Decision* __restrict__ dec,
+                                                                  uint64_t* __restrict__ flags) {
+    __shared__ float box_lo[kSmallWarps][kSmallMax][3], box_hi[kSmallWarps][kSmallMax][3];
+    const int warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t k = blockIdx.x * kSmallWarps + static_cast<uint32_t>(warp);
+    if (k >= n_list) return;   // the whole warp
+    const uint32_t ci = list[k];
+    const Cell c = cells[ci];
+    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+    const bool mine = lane < c.count;
+    const bool kept = mine && clip_to(verts, tri_box, refs[c.begin + lane], c, lo, hi);
+    const unsigned km = __ballot_sync(0xFFFFFFFFu, kept);
+    const uint32_t n = static_cast<uint32_t>(__popc(km));
+    if (kept) {
+        const uint32_t slot = static_cast<uint32_t>(__popc(km & ((1u << lane) - 1u)));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            box_lo[warp][slot][a] = lo[a];
+            box_hi[warp][slot][a] = hi[a];
+        }
+    }
+    __syncwarp();
+    const float sa = surface(c.lo, c.hi);
+    float bc = 3.4e38f, bp = 0.f;
+    int ba = 3, bpl = 0;
+    uint32_t bnl = 0, bnr = 0;
+    if (n > 3 && sa > 0.f) {
+        for (uint32_t t = lane; t < 6 * n; t += 32) {
+            const int a = static_cast<int>(t / (2 * n));
+            const uint32_t j = (t % (2 * n)) >> 1;
+            const float pos = (t & 1u) ? box_hi[warp][j][a] : box_lo[warp][j][a];
+            if (!(pos >= c.lo[a] && pos <= c.hi[a])) continue;
+            uint32_t nl = 0, nr = 0, np = 0;
+            for (uint32_t q = 0; q < n; ++q) {
+                const float blo = box_lo[warp][q][a], bhi = box_hi[warp][q][a];
+                nl += blo < pos ? 1u : 0u;
+                nr += bhi > pos ? 1u : 0u;
+                np += (blo == pos && bhi == pos) ? 1u : 0u;
+            }
+            consider(c, sa, n, a, pos, nl, nr, np, bc, ba, bp, bpl, bnl, bnr);
+        }
+    }
+    // better() is a total order, so the warp's best does not depend on which
+    // lane found which candidate
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oc = __shfl_down_sync(0xFFFFFFFFu, bc, off);
+        const int oa = __shfl_down_sync(0xFFFFFFFFu, ba, off);
+        const float op = __shfl_down_sync(0xFFFFFFFFu, bp, off);
+        const int opl = __shfl_down_sync(0xFFFFFFFFu, bpl, off);
+        const uint32_t onl = __shfl_down_sync(0xFFFFFFFFu, bnl, off);
+        const uint32_t onr = __shfl_down_sync(0xFFFFFFFFu, bnr, off);
+        if (better(oc, oa, op, opl, bc, ba, bp, bpl)) {
+            bc = oc;
+            ba = oa;
+            bp = op;
+            bpl = opl;
+            bnl = onl;
+            bnr = onr;
+        }
+    }
+    Decision r{0, 0, 0.f, n, 1};
+    if (lane == 0 && n > 3 && c.depth < kMaxBuildDepth && !last_level && ba < 3) {
+        if (!(kCostIntersection * static_cast<float>(n) < bc)) {   // the termination test of k_level
+            r.split = 1;
+            r.axis = ba;
+            r.pos = bp;
+            r.planar_left = bpl;
+        }
+    }
+    r.split = __shfl_sync(0xFFFFFFFFu, r.split, 0);
+    r.axis = __shfl_sync(0xFFFFFFFFu, r.axis, 0);
+    r.pos = __shfl_sync(0xFFFFFFFFu, r.pos, 0);
+    r.planar_left = __shfl_sync(0xFFFFFFFFu, r.planar_left, 0);
+    if (lane == 0) dec[ci] = r;
+    if (mine) {
+        uint64_t f = 0;
+        if (kept) {
+            if (!r.split) {
+                f = 1;
+            } else {
+                const bool pl = r.planar_left != 0;
+                const bool gl = goes_left(lo[r.axis], hi[r.axis], r.pos, pl);
+                const bool gr = goes_right(lo[r.axis], hi[r.axis], r.pos, pl);
+                f = (gl ? 1ull : 0ull) | (gr ? (1ull << 32) : 0ull);
+            }
+        }
+        flags[c.begin + lane] = f;
     }
 }
 
@@ -444,38 +549,64 @@ __global__ void k_scan_total(T* __restrict__ out, uint32_t n, const T* __restric
     out[n] = n ? out[n - 1] + in[n - 1] : T(0);
 }
 
-struct Scratch {
-    std::vector<void*> bufs;
-    ~Scratch() {
-        for (void* p : bufs) cudaFree(p);
+// Device buffers of the build, by slot, kept for the whole build and grown
+// (by at least half) only when a level needs more: levels reuse them instead
+// of allocating and freeing their own. Growing frees the old buffer, which
+// waits for the work queued on it.
+struct Arena {
+    struct Slot {
+        void* p = nullptr;
+        size_t bytes = 0;
+    };
+    std::vector<Slot> slots;
+    ~Arena() {
+        for (Slot& s : slots)
+            if (s.p) cudaFree(s.p);
     }
-    template <class T> cudaError_t alloc(T** p, size_t count) {
-        *p = nullptr;
-        if (count == 0) count = 1;
-        void* q = nullptr;
-        const cudaError_t e = cudaMalloc(&q, count * sizeof(T));
-        if (e == cudaSuccess) {
-            bufs.push_back(q);
-            *p = static_cast<T*>(q);
+    template <class T> cudaError_t get(size_t id, T** out, size_t count) {
+        *out = nullptr;
+        if (slots.size() <= id) slots.resize(id + 1);
+        Slot& s = slots[id];
+        const size_t need = std::max<size_t>(count, 1) * sizeof(T);
+        if (s.bytes < need) {
+            if (s.p) cudaFree(s.p);
+            s.p = nullptr;
+            s.bytes = 0;
+            const size_t cap = std::max(need, s.bytes + s.bytes / 2);
+            const cudaError_t e = cudaMalloc(&s.p, cap);
+            if (e != cudaSuccess) {
+                s.p = nullptr;
+                return e;
+            }
+            s.bytes = cap;
         }
-        return e;
+        *out = static_cast<T*>(s.p);
+        return cudaSuccess;
     }
 };
 
+// Arena slots. A scan at recursion depth k uses kSlotScan + 2k and + 2k + 1.
+enum : size_t {
+    kSlotVerts, kSlotBoxes, kSlotCells0, kSlotCells1, kSlotRefs0, kSlotRefs1, kSlotRefCell0, kSlotRefCell1,
+    kSlotSmall0, kSlotSmall1, kSlotLarge0, kSlotLarge1, kSlotDec, kSlotFlags, kSlotFscan, kSlotNChild, kSlotNNext,
+    kSlotNLeaf, kSlotChildBase, kSlotNextBase, kSlotLeafBase, kSlotLeafPool, kSlotLevelNodes, kSlotLists, kSlotScan
+};
+
 // out has n + 1 elements; in and out may not alias.
-template <class T> cudaError_t scan_exclusive(const T* in, uint32_t n, T* out, cudaStream_t st, Scratch& scratch) {
+template <class T>
+cudaError_t scan_exclusive(const T* in, uint32_t n, T* out, cudaStream_t st, Arena& arena, size_t slot = kSlotScan) {
     if (n == 0) {
         k_scan_total<T><<<1, 1, 0, st>>>(out, 0, in);
         return cudaGetLastError();
     }
     const uint32_t blocks = (n + kScanBlock - 1) / kScanBlock;
     T *sums = nullptr, *offs = nullptr;
-    cudaError_t e = scratch.alloc(&sums, blocks);
-    if (e == cudaSuccess) e = scratch.alloc(&offs, size_t(blocks) + 1);
+    cudaError_t e = arena.get(slot, &sums, blocks);
+    if (e == cudaSuccess) e = arena.get(slot + 1, &offs, size_t(blocks) + 1);
     if (e != cudaSuccess) return e;
     k_scan_block<T><<<blocks, kScanThreads, 0, st>>>(in, n, out, sums);
     if (blocks > 1) {
-        e = scan_exclusive<T>(sums, blocks, offs, st, scratch);
+        e = scan_exclusive<T>(sums, blocks, offs, st, arena, slot + 2);
         if (e != cudaSuccess) return e;
         k_scan_add<T><<<(n + 255) / 256, 256, 0, st>>>(out, n, offs);
     }
@@ -505,13 +636,36 @@ __global__ void k_counts(const Cell* __restrict__ cells, const Decision* __restr
     }
 }
 
+// Reserves n slots of *counter for this lane: one atomicAdd per warp.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+#pragma unroll
+    for (int k = 1; k < 32; k <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, k);
+        if (lane >= static_cast<uint32_t>(k)) incl += v;
+    }
+    uint32_t base = 0;
+    if (lane == 31 && incl) base = atomicAdd(counter, incl);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    return base + incl - n;
+}
+
+// The next level's cells and BFS records of this level's nodes; the children
+// are also listed by size for the next level's two kernels (lists[0] counts
+// and small_list holds cells of at most kSmallMax references, lists[1] and
+// large_list the others).
 __global__ void k_children(const Cell* __restrict__ cells, const Decision* __restrict__ dec,
                            const uint64_t* __restrict__ fscan, uint32_t n, const uint32_t* __restrict__ child_base,
                            const uint32_t* __restrict__ next_base, const uint32_t* __restrict__ leaf_base,
                            uint32_t leaf_offset, int32_t next_level_offset, Cell* __restrict__ next_cells,
-                           BfsNode* __restrict__ out) {
+                           BfsNode* __restrict__ out, uint32_t* __restrict__ lists, uint32_t* __restrict__ small_list,
+                           uint32_t* __restrict__ large_list) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // every lane takes part in the list appends; lanes past n add nothing
+    uint32_t child[2] = {0, 0}, count[2] = {0, 0};
+    uint32_t n_children = 0;
+    if (i < n) {
     const Cell c = cells[i];
     const Decision d = dec[i];
     const uint64_t a = fscan[c.begin], b = fscan[c.begin + c.count];
@@ -529,6 +683,8 @@ __global__ void k_children(const Cell* __restrict__ cells, const Decision* __res
             l.depth = child_depth;
             next_cells[slot] = l;
             r.left = next_level_offset + static_cast<int32_t>(slot);
+            child[n_children] = slot;
+            count[n_children++] = nl;
             ++slot;
         }
         if (nr) {
@@ -539,12 +695,23 @@ __global__ void k_children(const Cell* __restrict__ cells, const Decision* __res
             rr.depth = child_depth;
             next_cells[slot] = rr;
             r.right = next_level_offset + static_cast<int32_t>(slot);
+            child[n_children] = slot;
+            count[n_children++] = nr;
         }
     } else {
         r.leaf_begin = leaf_offset + leaf_base[i];
         r.leaf_count = nl;
     }
     out[i] = r;
+    }
+    uint32_t n_small = 0;
+    for (uint32_t k = 0; k < n_children; ++k) n_small += count[k] <= kSmallMax ? 1u : 0u;
+    uint32_t small_at = warp_reserve(lists, n_small);
+    uint32_t large_at = warp_reserve(lists + 1, n_children - n_small);
+    for (uint32_t k = 0; k < n_children; ++k) {
+        if (count[k] <= kSmallMax) small_list[small_at++] = child[k];
+        else large_list[large_at++] = child[k];
+    }
 }
 
 __global__ void k_scatter(const Cell* __restrict__ cells, const Decision* __restrict__ dec,
@@ -673,7 +840,7 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
     }
     if (cudaSetDevice(turner::ctx_device(ctx)) != cudaSuccess) return TURNER_ERR_CUDA;
     cudaStream_t st = turner::ctx_stream(ctx);
-    Scratch keep;   // lives for the whole build
+    Arena arena;   // every device buffer of the build
 #define GB_CK(call)                                                                              \
     do {                                                                                         \
         const cudaError_t e_ = (call);                                                           \
@@ -681,8 +848,8 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
                                                                       : TURNER_ERR_CUDA;         \
     } while (0)
     float *d_v = nullptr, *d_box = nullptr;
-    GB_CK(keep.alloc(&d_v, 9 * size_t(n_tris)));
-    GB_CK(keep.alloc(&d_box, 6 * size_t(n_tris)));
+    GB_CK(arena.get(kSlotVerts, &d_v, 9 * size_t(n_tris)));
+    GB_CK(arena.get(kSlotBoxes, &d_box, 6 * size_t(n_tris)));
     GB_CK(cudaMemcpyAsync(d_v, vertices, sizeof(float) * 9 * size_t(n_tris), cudaMemcpyHostToDevice, st));
     k_tri_boxes<<<(n_tris + 255) / 256, 256, 0, st>>>(d_v, n_tris, d_box);
     GB_CK(cudaGetLastError());
@@ -697,13 +864,18 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
     root.count = n_tris;
     root.depth = 0;
     uint32_t n_cells = 1, n_refs = n_tris;
+    // the root is the only cell of level 0, in the small or the large list
+    uint32_t n_small = n_tris <= kSmallMax ? 1u : 0u, n_large = 1u - n_small;
     Cell* cells = nullptr;
-    uint32_t *refs = nullptr, *ref_cell = nullptr;
-    Scratch cur;    // the current level's cells and references
-    GB_CK(cur.alloc(&cells, 1));
-    GB_CK(cur.alloc(&refs, n_refs));
-    GB_CK(cur.alloc(&ref_cell, n_refs));
+    uint32_t *refs = nullptr, *ref_cell = nullptr, *small_list = nullptr, *large_list = nullptr;
+    GB_CK(arena.get(kSlotCells0, &cells, 1));
+    GB_CK(arena.get(kSlotRefs0, &refs, n_refs));
+    GB_CK(arena.get(kSlotRefCell0, &ref_cell, n_refs));
+    GB_CK(arena.get(kSlotSmall0, &small_list, 1));
+    GB_CK(arena.get(kSlotLarge0, &large_list, 1));
     GB_CK(cudaMemcpyAsync(cells, &root, sizeof(Cell), cudaMemcpyHostToDevice, st));
+    GB_CK(cudaMemsetAsync(small_list, 0, sizeof(uint32_t), st));
+    GB_CK(cudaMemsetAsync(large_list, 0, sizeof(uint32_t), st));
     k_iota<<<(n_refs + 255) / 256, 256, 0, st>>>(refs, n_refs);
     GB_CK(cudaMemsetAsync(ref_cell, 0, sizeof(uint32_t) * n_refs, st));
 
@@ -716,29 +888,39 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
     // flattened, so cells count only two-sided splits as depth; the number
     // of levels is bounded separately
     for (uint32_t level = 0; n_cells > 0; ++level) {
-        Scratch lvl;
+        // this level's cells, references and lists are in the slots of its
+        // parity; the next level's go to the others
+        const size_t nxt = (level + 1) & 1u;
         Decision* dec = nullptr;
         uint64_t *flags = nullptr, *fscan = nullptr;
         uint32_t *n_child = nullptr, *n_next = nullptr, *n_leaf = nullptr, *child_base = nullptr,
-                 *next_base = nullptr, *leaf_base = nullptr;
-        GB_CK(lvl.alloc(&dec, n_cells));
-        GB_CK(lvl.alloc(&flags, n_refs));
-        GB_CK(lvl.alloc(&fscan, size_t(n_refs) + 1));
-        GB_CK(lvl.alloc(&n_child, n_cells));
-        GB_CK(lvl.alloc(&n_next, n_cells));
-        GB_CK(lvl.alloc(&n_leaf, n_cells));
-        GB_CK(lvl.alloc(&child_base, size_t(n_cells) + 1));
-        GB_CK(lvl.alloc(&next_base, size_t(n_cells) + 1));
-        GB_CK(lvl.alloc(&leaf_base, size_t(n_cells) + 1));
-        k_level<<<n_cells, kLevelThreads, 0, st>>>(cells, refs, d_v, d_box, level + 1 >= kMaxLevels, dec, flags);
+                 *next_base = nullptr, *leaf_base = nullptr, *lists = nullptr;
+        GB_CK(arena.get(kSlotDec, &dec, n_cells));
+        GB_CK(arena.get(kSlotFlags, &flags, n_refs));
+        GB_CK(arena.get(kSlotFscan, &fscan, size_t(n_refs) + 1));
+        GB_CK(arena.get(kSlotNChild, &n_child, n_cells));
+        GB_CK(arena.get(kSlotNNext, &n_next, n_cells));
+        GB_CK(arena.get(kSlotNLeaf, &n_leaf, n_cells));
+        GB_CK(arena.get(kSlotChildBase, &child_base, size_t(n_cells) + 1));
+        GB_CK(arena.get(kSlotNextBase, &next_base, size_t(n_cells) + 1));
+        GB_CK(arena.get(kSlotLeafBase, &leaf_base, size_t(n_cells) + 1));
+        GB_CK(arena.get(kSlotLists, &lists, 2));
+        const bool last = level + 1 >= kMaxLevels;
+        if (n_large) {
+            k_level<<<n_large, kLevelThreads, 0, st>>>(cells, large_list, refs, d_v, d_box, last, dec, flags);
+        }
+        if (n_small) {
+            k_level_small<<<(n_small + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, 0, st>>>(
+                cells, small_list, n_small, refs, d_v, d_box, last, dec, flags);
+        }
         GB_CK(cudaGetLastError());
-        GB_CK(scan_exclusive<uint64_t>(flags, n_refs, fscan, st, lvl));
+        GB_CK(scan_exclusive<uint64_t>(flags, n_refs, fscan, st, arena));
         const unsigned gc = (n_cells + 255) / 256;
         k_counts<<<gc, 256, 0, st>>>(cells, dec, fscan, n_cells, n_child, n_next, n_leaf);
         GB_CK(cudaGetLastError());
-        GB_CK(scan_exclusive<uint32_t>(n_child, n_cells, child_base, st, lvl));
-        GB_CK(scan_exclusive<uint32_t>(n_next, n_cells, next_base, st, lvl));
-        GB_CK(scan_exclusive<uint32_t>(n_leaf, n_cells, leaf_base, st, lvl));
+        GB_CK(scan_exclusive<uint32_t>(n_child, n_cells, child_base, st, arena));
+        GB_CK(scan_exclusive<uint32_t>(n_next, n_cells, next_base, st, arena));
+        GB_CK(scan_exclusive<uint32_t>(n_leaf, n_cells, leaf_base, st, arena));
         uint32_t totals[3] = {0, 0, 0};
         GB_CK(cudaMemcpyAsync(&totals[0], child_base + n_cells, 4, cudaMemcpyDeviceToHost, st));
         GB_CK(cudaMemcpyAsync(&totals[1], next_base + n_cells, 4, cudaMemcpyDeviceToHost, st));
@@ -748,17 +930,20 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         if (uint64_t(bfs.size()) + n_cells + next_cells_n >= (1ull << 31)) return TURNER_ERR_TOO_LARGE;
 
         Cell* next_cells = nullptr;
-        uint32_t *next_refs = nullptr, *next_ref_cell = nullptr, *leaf_pool = nullptr;
+        uint32_t *next_refs = nullptr, *next_ref_cell = nullptr, *next_small = nullptr, *next_large = nullptr,
+                 *leaf_pool = nullptr;
         BfsNode* level_nodes = nullptr;
-        Scratch next;   // the next level's cells and references
-        GB_CK(next.alloc(&next_cells, next_cells_n));
-        GB_CK(next.alloc(&next_refs, next_refs_n));
-        GB_CK(next.alloc(&next_ref_cell, next_refs_n));
-        GB_CK(lvl.alloc(&leaf_pool, leaf_n));
-        GB_CK(lvl.alloc(&level_nodes, n_cells));
+        GB_CK(arena.get(kSlotCells0 + nxt, &next_cells, next_cells_n));
+        GB_CK(arena.get(kSlotRefs0 + nxt, &next_refs, next_refs_n));
+        GB_CK(arena.get(kSlotRefCell0 + nxt, &next_ref_cell, next_refs_n));
+        GB_CK(arena.get(kSlotSmall0 + nxt, &next_small, next_cells_n));
+        GB_CK(arena.get(kSlotLarge0 + nxt, &next_large, next_cells_n));
+        GB_CK(arena.get(kSlotLeafPool, &leaf_pool, leaf_n));
+        GB_CK(arena.get(kSlotLevelNodes, &level_nodes, n_cells));
+        GB_CK(cudaMemsetAsync(lists, 0, 2 * sizeof(uint32_t), st));
         const int32_t next_offset = static_cast<int32_t>(bfs.size() + n_cells);
         k_children<<<gc, 256, 0, st>>>(cells, dec, fscan, n_cells, child_base, next_base, leaf_base, leaf_total,
-                                       next_offset, next_cells, level_nodes);
+                                       next_offset, next_cells, level_nodes, lists, next_small, next_large);
         if (n_refs) {
             k_scatter<<<(n_refs + 255) / 256, 256, 0, st>>>(cells, dec, refs, ref_cell, flags, fscan, n_refs,
                                                             child_base, next_base, leaf_base, next_refs,
@@ -773,21 +958,25 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         } catch (const std::bad_alloc&) {
             return TURNER_ERR_OUT_OF_MEMORY;
         }
+        uint32_t counts[2] = {0, 0};
         GB_CK(cudaMemcpyAsync(bfs.data() + base, level_nodes, sizeof(BfsNode) * n_cells, cudaMemcpyDeviceToHost, st));
         if (leaf_n)
             GB_CK(cudaMemcpyAsync(pool_parts.back().get(), leaf_pool, sizeof(uint32_t) * leaf_n,
                                   cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaMemcpyAsync(counts, lists, sizeof(counts), cudaMemcpyDeviceToHost, st));
         GB_CK(cudaStreamSynchronize(st));
         leaf_total += leaf_n;
-        // the next level becomes current; this level's buffers (now in
-        // `next`, and `lvl`) are freed at the end of the iteration, after the
-        // synchronisation above
+        // the next level becomes current
         cells = next_cells;
         refs = next_refs;
         ref_cell = next_ref_cell;
+        small_list = next_small;
+        large_list = next_large;
         n_cells = next_cells_n;
         n_refs = next_refs_n;
-        std::swap(cur.bufs, next.bufs);
+        n_small = counts[0];
+        n_large = counts[1];
+        if (n_small + n_large != n_cells) return TURNER_ERR_CUDA;
     }
 #undef GB_CK
     std::vector<uint32_t> pool;
