@@ -1101,7 +1101,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
                 if (t.min_blocks == v || t.block != 128) return false;
                 t.min_blocks = v;
                 return true;
-            }, std::vector<uint32_t>{0, 10, 16});
+            }, std::vector<uint32_t>{0, 12, 16});
     if (s == TURNER_OK)
         s = try_value([&](turner_tuning& t, int v) { if (t.persistent == v) return false; t.persistent = v; return true; },
                       std::vector<int>{0});
