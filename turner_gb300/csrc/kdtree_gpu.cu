@@ -569,10 +569,10 @@ struct Arena {
         Slot& s = slots[id];
         const size_t need = std::max<size_t>(count, 1) * sizeof(T);
         if (s.bytes < need) {
+            const size_t cap = std::max(need, s.bytes + s.bytes / 2);
             if (s.p) cudaFree(s.p);
             s.p = nullptr;
             s.bytes = 0;
-            const size_t cap = std::max(need, s.bytes + s.bytes / 2);
             const cudaError_t e = cudaMalloc(&s.p, cap);
             if (e != cudaSuccess) {
                 s.p = nullptr;
