@@ -615,7 +615,7 @@ def main() -> None:
             "gpu_launches": int(launches),
             "rays_per_step": int(rays // args.steps), "shadow_rays_per_step": int(shadow // args.steps),
             # the same timed region, counted other ways (all ranks: this rank's counts x world size)
-            "mpaths_per_s": round(world * WIDTH * HEIGHT * SPP * MC * args.steps / t_max / 1e6, 3),
+            "mpaths_per_s": round(world * WIDTH * HEIGHT * SPP * args.steps / t_max / 1e6, 3),
             "mrays_incl_shadow_per_s": round(world * (rays + shadow) / t_max / 1e6, 3),
             "wall_ms_per_step": round(1000 * wall / args.steps, 3),
             "kernels_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in ktimes.items() if v[1]},
