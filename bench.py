@@ -447,10 +447,12 @@ def main() -> None:
     ap.add_argument("--views-spp", type=int, default=64)
     ap.add_argument("--views-train-s", type=float, default=3.0)
     ap.add_argument("--views-ref-spp", type=int, default=2048)
-    ap.add_argument("--guide-side", type=int, default=512)
-    ap.add_argument("--ref-spp", type=int, default=8192)
-    ap.add_argument("--pass-spp", type=int, default=4)
-    ap.add_argument("--budget", type=float, default=3.0)
+    # guide workload defaults: the indirect-lit room at 1024x1024 against a
+    # 16,384-spp FP64 reference, 10 s of equal wall time in 1-spp passes
+    ap.add_argument("--guide-side", type=int, default=1024)
+    ap.add_argument("--ref-spp", type=int, default=16384)
+    ap.add_argument("--pass-spp", type=int, default=1)
+    ap.add_argument("--budget", type=float, default=10.0)
     ap.add_argument("--train-fraction", type=float, default=0.3)
     ap.add_argument("--guide-records", type=int, default=1 << 16)
     ap.add_argument("--guide-lr", type=float, default=1e-3)
