@@ -253,8 +253,16 @@ def run_guide(args) -> None:
     # reference's own variance, which inflates both MSEs by the same amount
     t0 = time.perf_counter()
     half = max(1, args.ref_spp // 512)
-    ref_a, spp_a = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 424242), half)
-    ref_b, spp_b = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 525252), half)
+    cache = Path(args.ref_cache) if args.ref_cache else None
+    cache_key = f"{side}-{depth}-{half}"
+    if cache is not None and cache.exists() and str(np.load(cache)["key"]) == cache_key:
+        z = np.load(cache)
+        ref_a, ref_b, spp_a, spp_b = z["a"], z["b"], int(z["spp_a"]), int(z["spp_b"])
+    else:
+        ref_a, spp_a = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 424242), half)
+        ref_b, spp_b = ctx.accumulate(job(tg.SAMPLING_COSINE, 256, 525252), half)
+        if cache is not None:
+            np.savez(cache, a=ref_a, b=ref_b, spp_a=spp_a, spp_b=spp_b, key=cache_key)
     ref_s = time.perf_counter() - t0
     ref, ref_spp = 0.5 * (ref_a + ref_b), spp_a + spp_b
     ref_var = float(((ref_a[..., :3] - ref_b[..., :3]) ** 2).mean() / 4)
@@ -453,10 +461,11 @@ def main() -> None:
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--pass-spp", type=int, default=1)
     ap.add_argument("--budget", type=float, default=10.0)
-    ap.add_argument("--train-fraction", type=float, default=0.3)
+    ap.add_argument("--ref-cache", default="", help="guide: .npz file that keeps the FP64 reference between runs")
+    ap.add_argument("--train-fraction", type=float, default=0.2)
     ap.add_argument("--guide-records", type=int, default=1 << 16)
     ap.add_argument("--guide-lr", type=float, default=1e-3)
-    ap.add_argument("--guide-steps", type=int, default=4, help="Adam steps per training pass")
+    ap.add_argument("--guide-steps", type=int, default=16, help="Adam steps per training pass")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")
