@@ -454,7 +454,7 @@ def main() -> None:
     ap.add_argument("--views-radius", type=float, default=4.0)
     ap.add_argument("--views-spp", type=int, default=64)
     ap.add_argument("--views-train-s", type=float, default=3.0)
-    ap.add_argument("--views-ref-spp", type=int, default=2048)
+    ap.add_argument("--views-ref-spp", type=int, default=8192)
     # guide workload defaults: the indirect-lit room at 1024x1024 against a
     # 16,384-spp FP64 reference, 10 s of equal wall time in 1-spp passes
     ap.add_argument("--guide-side", type=int, default=1024)
