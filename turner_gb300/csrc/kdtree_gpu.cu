@@ -777,6 +777,16 @@ int flatten(const std::vector<BfsNode>& bfs, const std::vector<uint32_t>& pool, 
         eff[k] = (l >= 0 && r >= 0) ? static_cast<int32_t>(k) : (l >= 0 ? l : r);
     }
     if (n == 0 || eff[0] < 0) return TURNER_ERR_INVALID_ARG;
+    // words of the flattened tree: one per kept inner node, count / 2 + 1 per
+    // leaf (pairs, then a half-empty leaf or the sentinel); reserved up front
+    // so that a tree of tens of millions of words is not copied while it grows
+    size_t n_words = 0;
+    for (size_t k = 0; k < n; ++k) {
+        const BfsNode& b = bfs[k];
+        if (eff[k] != static_cast<int32_t>(k)) continue;   // dropped, or stands for nothing
+        n_words += b.split ? 1u : b.leaf_count / 2 + 1;
+    }
+    words.reserve(n_words);
     constexpr uint32_t kNone = 0xFFFFFFFFu >> 2;
     struct Item {
         int32_t node;
@@ -880,8 +890,7 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
     GB_CK(cudaMemsetAsync(ref_cell, 0, sizeof(uint32_t) * n_refs, st));
 
     std::vector<BfsNode> bfs;
-    std::vector<std::unique_ptr<uint32_t[]>> pool_parts;
-    std::vector<uint32_t> pool_sizes;
+    std::vector<uint32_t> pool;   // leaf references of all levels, in level order
     uint32_t leaf_total = 0;
     // the leaf pool grows in pieces, one per level (host copies)
     // an empty-space cut leaves one child and is dropped when the tree is
@@ -953,15 +962,14 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         const size_t base = bfs.size();
         try {
             bfs.resize(base + n_cells);
-            pool_parts.emplace_back(new uint32_t[std::max<uint32_t>(1, leaf_n)]);
-            pool_sizes.push_back(leaf_n);
+            pool.resize(size_t(leaf_total) + leaf_n);
         } catch (const std::bad_alloc&) {
             return TURNER_ERR_OUT_OF_MEMORY;
         }
         uint32_t counts[2] = {0, 0};
         GB_CK(cudaMemcpyAsync(bfs.data() + base, level_nodes, sizeof(BfsNode) * n_cells, cudaMemcpyDeviceToHost, st));
         if (leaf_n)
-            GB_CK(cudaMemcpyAsync(pool_parts.back().get(), leaf_pool, sizeof(uint32_t) * leaf_n,
+            GB_CK(cudaMemcpyAsync(pool.data() + leaf_total, leaf_pool, sizeof(uint32_t) * leaf_n,
                                   cudaMemcpyDeviceToHost, st));
         GB_CK(cudaMemcpyAsync(counts, lists, sizeof(counts), cudaMemcpyDeviceToHost, st));
         GB_CK(cudaStreamSynchronize(st));
@@ -979,14 +987,6 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         if (n_small + n_large != n_cells) return TURNER_ERR_CUDA;
     }
 #undef GB_CK
-    std::vector<uint32_t> pool;
-    try {
-        pool.reserve(leaf_total);
-        for (size_t k = 0; k < pool_parts.size(); ++k)
-            pool.insert(pool.end(), pool_parts[k].get(), pool_parts[k].get() + pool_sizes[k]);
-    } catch (const std::bad_alloc&) {
-        return TURNER_ERR_OUT_OF_MEMORY;
-    }
     int status;
     try {
         status = flatten(bfs, pool, tree->nodes, tree->height);
