@@ -102,3 +102,7 @@ def test_cli_help_and_flag_errors():
     assert r.returncode == 1
     r = subprocess.run([str(cli), "room", "-d", "0"], capture_output=True, text=True)   # TracerConfig::check
     assert r.returncode == 1
+    # a tree file is keyed by the triangles alone: GPU-built trees stay out of the cache
+    r = subprocess.run([str(cli), "room", "--gpu-kdtree", "--kdtree-cache", "/nonexistent"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "--gpu-kdtree" in r.stderr

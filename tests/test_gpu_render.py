@@ -209,6 +209,21 @@ def test_tree_file_upload_and_cli_cache(ctx, tmp_path):
     assert r1.stdout == r2.stdout and r1.stdout.startswith("P3\n32 32\n255\n")
 
 
+def test_cli_gpu_kdtree():
+    """--gpu-kdtree renders through a tree built on the GPU: the same image as
+    the reference's tree up to exact ties (coincident faces)."""
+    import subprocess
+    cli = tg.LIB_DIR / "turner_pathtracer"
+    base = [str(cli), "sphere:3", "-w", "48", "-p", "4", "-m", "1"]
+    host = subprocess.run(base, capture_output=True, text=True)
+    gpu = subprocess.run(base + ["--gpu-kdtree"], capture_output=True, text=True)
+    assert host.returncode == 0 and gpu.returncode == 0, host.stderr + gpu.stderr
+    assert gpu.stdout.startswith("P3\n48 48\n255\n")
+    a = np.array(host.stdout.split()[4:], np.int32)
+    b = np.array(gpu.stdout.split()[4:], np.int32)
+    assert a.shape == b.shape and (np.abs(a - b) <= 1).mean() >= 0.99
+
+
 CLASSIC = {
     # golden name: (scene, job arguments)
     "mirror_raytrace": (dict(kind=tg.SCENE_MIRROR_ROOM),

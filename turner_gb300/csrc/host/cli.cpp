@@ -46,6 +46,9 @@ GB300 options:
   --device=<int>                    CUDA device [default: 0].
   --kdtree-cache=<dir>              Directory of content-keyed kd-tree files: load the
                                     scene's tree from it, or build and store it.
+  --gpu-kdtree                      Build the kd-tree on the GPU (its own SAH planes,
+                                    not the reference's node words; same closest hits).
+                                    Not with --kdtree-cache.
 
 Scenes: room | sphere[:DETAIL] | soup:COUNT[:SEED] | baffle[:DETAIL] | baffle-sphere[:DETAIL] | mirror
 )";
@@ -68,6 +71,7 @@ struct Options {
     float shadow = 0.5f, max_visibility = 2.f;
     int device = 0;
     std::string kdtree_cache;
+    bool gpu_kdtree = false;
 };
 
 bool take(int& i, int argc, char** argv, const char* s, const char* l, std::string& val) {
@@ -133,6 +137,7 @@ int parse(int argc, char** argv, Options& o) {
         else if (a == "--fast") o.fast = true;
         else if (take(i, argc, argv, nullptr, "--device", v)) o.device = std::stoi(v);
         else if (take(i, argc, argv, nullptr, "--kdtree-cache", v)) o.kdtree_cache = v;
+        else if (a == "--gpu-kdtree") o.gpu_kdtree = true;
         else if (!a.empty() && a[0] != '-' && o.scene.empty()) o.scene = a;
         else return 2;
     }
@@ -140,6 +145,8 @@ int parse(int argc, char** argv, Options& o) {
     if (o.scene.empty() || !(o.aspect > 0) || o.exposure < 0 || o.depth <= 0 || o.pixel_samples < 1 || o.mc < 0 ||
         o.width < 1 || !(o.shadow >= 0.f && o.shadow <= 1.f) || !(o.max_visibility >= 0.f))
         return 2;
+    // a cache file is keyed by the triangles alone, so it cannot tell the two builders' trees apart
+    if (o.gpu_kdtree && !o.kdtree_cache.empty()) return 2;
     return 0;
 }
 
@@ -182,13 +189,24 @@ int main(int argc, char** argv) {
         std::cerr << "scene: " << turner_strerror(st) << std::endl;
         return 1;
     }
+    turner_ctx* ctx = nullptr;
+    st = turner_create(&ctx, o.device);
+    if (st != TURNER_OK) {
+        std::cerr << "device: " << turner_strerror(st) << std::endl;
+        return 1;
+    }
     std::cerr << "Loading triangles and building kd-tree..." << std::endl;
     turner_kdtree* tree = nullptr;
     const auto t_tree = clock::now();
     int from_cache = 0;
-    st = turner_kdtree_build_cached(turner_mesh_vertices(mesh), turner_mesh_normals(mesh), turner_mesh_diffuse(mesh),
-                                    turner_mesh_num_triangles(mesh), 0,
-                                    o.kdtree_cache.empty() ? nullptr : o.kdtree_cache.c_str(), &tree, &from_cache);
+    if (o.gpu_kdtree) {
+        st = turner_kdtree_build_gpu(ctx, turner_mesh_vertices(mesh), turner_mesh_normals(mesh),
+                                     turner_mesh_diffuse(mesh), turner_mesh_num_triangles(mesh), &tree);
+    } else {
+        st = turner_kdtree_build_cached(turner_mesh_vertices(mesh), turner_mesh_normals(mesh),
+                                        turner_mesh_diffuse(mesh), turner_mesh_num_triangles(mesh), 0,
+                                        o.kdtree_cache.empty() ? nullptr : o.kdtree_cache.c_str(), &tree, &from_cache);
+    }
     if (st != TURNER_OK) {
         std::cerr << "kd-tree: " << turner_strerror(st) << std::endl;
         return 1;
@@ -198,13 +216,6 @@ int main(int argc, char** argv) {
     const double tree_ms = std::chrono::duration<double, std::milli>(clock::now() - t_tree).count();
     std::cerr << "KDTree runtime: " << static_cast<long>(tree_ms) << std::endl;
     const double load_s = std::chrono::duration<double>(clock::now() - t_load).count();
-
-    turner_ctx* ctx = nullptr;
-    st = turner_create(&ctx, o.device);
-    if (st != TURNER_OK) {
-        std::cerr << "device: " << turner_strerror(st) << std::endl;
-        return 1;
-    }
     uint32_t scene_id = 0;
     st = turner_upload_kdtree(ctx, tree, &scene_id);
     if (st != TURNER_OK) {
