@@ -39,9 +39,12 @@
 // adjacent, leaves two ids per word, half-empty leaf or sentinel at the end of
 // a run), dropping empty children as KDTree's builder does.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <new>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -763,67 +766,112 @@ inline uint32_t float_bits(float f) {
 // FlatNode words (lib/kdtree.h:62-154) of the breadth-first tree, depth
 // first with the left child adjacent; empty children are dropped and a node
 // left with one child is replaced by it, as KDTree's builder does.
+//
+// Every kept node's subtree occupies a known number of words (one per inner
+// node, count / 2 + 1 per leaf), so its position follows from its parent's:
+// the left child right after the parent, the right child after the whole
+// left subtree. Subtrees are therefore written independently, on all host
+// threads, into a vector sized once.
 int flatten(const std::vector<BfsNode>& bfs, const std::vector<uint32_t>& pool, std::vector<uint64_t>& words,
             uint32_t& height) {
     const size_t n = bfs.size();
+    if (n == 0) return TURNER_ERR_INVALID_ARG;
     std::vector<int32_t> eff(n, -1);   // the node that stands for i (-1: empty)
+    std::vector<uint64_t> size(n, 0);  // words of the subtree of a kept node
+    // children come after their parents in breadth-first order
     for (size_t k = n; k-- > 0;) {
         const BfsNode& b = bfs[k];
         if (!b.split) {
-            eff[k] = b.leaf_count ? static_cast<int32_t>(k) : -1;
+            if (b.leaf_count) {
+                eff[k] = static_cast<int32_t>(k);
+                size[k] = b.leaf_count / 2 + 1;
+            }
             continue;
         }
         const int32_t l = b.left >= 0 ? eff[b.left] : -1, r = b.right >= 0 ? eff[b.right] : -1;
-        eff[k] = (l >= 0 && r >= 0) ? static_cast<int32_t>(k) : (l >= 0 ? l : r);
-    }
-    if (n == 0 || eff[0] < 0) return TURNER_ERR_INVALID_ARG;
-    // words of the flattened tree: one per kept inner node, count / 2 + 1 per
-    // leaf (pairs, then a half-empty leaf or the sentinel); reserved up front
-    // so that a tree of tens of millions of words is not copied while it grows
-    size_t n_words = 0;
-    for (size_t k = 0; k < n; ++k) {
-        const BfsNode& b = bfs[k];
-        if (eff[k] != static_cast<int32_t>(k)) continue;   // dropped, or stands for nothing
-        n_words += b.split ? 1u : b.leaf_count / 2 + 1;
-    }
-    words.reserve(n_words);
-    constexpr uint32_t kNone = 0xFFFFFFFFu >> 2;
-    struct Item {
-        int32_t node;
-        uint32_t parent;
-        uint32_t level;
-    };
-    std::vector<Item> st{{eff[0], kNone, 0}};
-    height = 0;
-    words.clear();
-    while (!st.empty()) {
-        const Item it = st.back();
-        st.pop_back();
-        const uint32_t idx = static_cast<uint32_t>(words.size());
-        if (it.parent != kNone) {
-            const uint64_t w = words[it.parent];
-            words[it.parent] = (w & 0xFFFFFFFF00000000ull) | static_cast<uint32_t>(idx << 2 | static_cast<uint32_t>(w & 3u));
-        }
-        height = std::max(height, it.level);
-        const BfsNode& b = bfs[it.node];
-        if (b.split) {
-            words.push_back(static_cast<uint64_t>(float_bits(b.pos)) << 32 |
-                            static_cast<uint32_t>(kNone << 2 | static_cast<uint32_t>(b.axis)));
-            st.push_back({eff[b.right], idx, it.level + 1});
-            st.push_back({eff[b.left], kNone, it.level + 1});
+        if (l >= 0 && r >= 0) {
+            eff[k] = static_cast<int32_t>(k);
+            size[k] = 1 + size[l] + size[r];
         } else {
-            const uint32_t* ids = pool.data() + b.leaf_begin;
-            uint32_t i = 1;
-            for (; i < b.leaf_count; i += 2)
-                words.push_back(static_cast<uint64_t>(ids[i - 1]) << 32 | static_cast<uint64_t>(ids[i] << 2 | 3u));
-            if (i - 1 < b.leaf_count) {
-                words.push_back(static_cast<uint64_t>(ids[i - 1]) << 32 | static_cast<uint64_t>(kNone << 2 | 3u));
+            eff[k] = l >= 0 ? l : r;
+        }
+    }
+    if (eff[0] < 0) return TURNER_ERR_INVALID_ARG;
+    const uint64_t total = size[eff[0]];
+    if (total >= TURNER_MISS) return TURNER_ERR_TOO_LARGE;
+    words.assign(total, 0);
+    constexpr uint32_t kNone = 0xFFFFFFFFu >> 2;
+    struct Task {
+        int32_t node;
+        uint32_t pos;     // index of the subtree's first word
+        uint32_t level;   // depth of the subtree's root
+    };
+    auto inner_word = [&](const BfsNode& b, uint32_t right) {
+        return static_cast<uint64_t>(float_bits(b.pos)) << 32 | static_cast<uint32_t>(right << 2 | static_cast<uint32_t>(b.axis));
+    };
+    // writes a subtree depth first; returns its height
+    auto emit = [&](Task root) {
+        uint32_t h = 0;
+        std::vector<Task> st{root};
+        while (!st.empty()) {
+            const Task t = st.back();
+            st.pop_back();
+            h = std::max(h, t.level);
+            const BfsNode& b = bfs[t.node];
+            if (b.split) {
+                const int32_t l = eff[b.left], r = eff[b.right];
+                const uint32_t rpos = t.pos + 1 + static_cast<uint32_t>(size[l]);
+                words[t.pos] = inner_word(b, rpos);
+                st.push_back({r, rpos, t.level + 1});
+                st.push_back({l, t.pos + 1, t.level + 1});
             } else {
-                words.push_back(0);   // sentinel: ends the run
+                const uint32_t* ids = pool.data() + b.leaf_begin;
+                uint32_t w = t.pos, i = 1;
+                for (; i < b.leaf_count; i += 2)
+                    words[w++] = static_cast<uint64_t>(ids[i - 1]) << 32 | static_cast<uint64_t>(ids[i] << 2 | 3u);
+                words[w] = i - 1 < b.leaf_count
+                               ? static_cast<uint64_t>(ids[i - 1]) << 32 | static_cast<uint64_t>(kNone << 2 | 3u)
+                               : 0;   // sentinel: ends the run
             }
         }
-        if (words.size() >= TURNER_MISS) return TURNER_ERR_TOO_LARGE;
+        return h;
+    };
+    // split the top of the tree into independent subtrees for the threads
+    const unsigned threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<Task> tasks{{eff[0], 0, 0}};
+    height = 0;
+    for (;;) {
+        size_t big = tasks.size();
+        for (size_t k = 0; k < tasks.size(); ++k) {
+            if (!bfs[tasks[k].node].split) continue;
+            if (big == tasks.size() || size[tasks[k].node] > size[tasks[big].node]) big = k;
+        }
+        if (big == tasks.size() || tasks.size() >= 8 * threads || size[tasks[big].node] < (1u << 16)) break;
+        const Task t = tasks[big];
+        const BfsNode& b = bfs[t.node];
+        const int32_t l = eff[b.left], r = eff[b.right];
+        const uint32_t rpos = t.pos + 1 + static_cast<uint32_t>(size[l]);
+        words[t.pos] = inner_word(b, rpos);
+        height = std::max(height, t.level);
+        tasks[big] = {l, t.pos + 1, t.level + 1};
+        tasks.push_back({r, rpos, t.level + 1});
     }
+    std::vector<uint32_t> heights(tasks.size(), 0);
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t k; (k = next.fetch_add(1)) < tasks.size();) heights[k] = emit(tasks[k]);
+    };
+    std::vector<std::thread> pool_threads;
+    for (unsigned k = 1; k < std::min<size_t>(threads, tasks.size()); ++k) {
+        try {
+            pool_threads.emplace_back(worker);
+        } catch (const std::system_error&) {
+            break;   // fewer threads: the remaining tasks run on the ones there are
+        }
+    }
+    worker();
+    for (auto& th : pool_threads) th.join();
+    for (uint32_t h : heights) height = std::max(height, h);
     return TURNER_OK;
 }
 
