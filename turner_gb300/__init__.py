@@ -470,7 +470,7 @@ class Context:
         _check(_lib().turner_set_tuning(self._h, C.byref(t)), "turner_set_tuning")
 
     def set_guide(self, guide: "Guide | None", train: bool = False, lr: float = 1e-3, records: int = 0,
-                  steps_per_pass: int = 1) -> None:
+                  steps_per_pass: int = 16) -> None:
         _check(_lib().turner_set_guide(self._h, guide._h if guide is not None else None, 1 if train else 0, lr,
                                        records), "turner_set_guide")
         _check(_lib().turner_set_guide_steps(self._h, steps_per_pass), "turner_set_guide_steps")

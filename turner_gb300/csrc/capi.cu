@@ -99,7 +99,7 @@ struct turner_ctx {
     bool guide_train = false;
     float guide_lr = 1e-3f;
     uint32_t guide_records = 1u << 18;   // training samples per pass
-    uint32_t guide_steps_per_pass = 1;    // Adam steps on each pass's samples
+    uint32_t guide_steps_per_pass = 16;   // Adam steps on each pass's samples
     DevBuf gfeat, gout, qa_rec, qb_rec, r_feat, r_dir, r_weight, r_path, r_lbefore, r_tafter, r_fcp, r_count;
     double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
