@@ -95,7 +95,7 @@ def test_gpu_tree_renders_like_the_reference_tree(ctx):
     assert abs(int(sa.rays) - int(sb.rays)) <= 0.005 * int(sb.rays)
 
 
-@pytest.mark.parametrize("name,visits,tests", [("sphere5", 0.75, 0.4), ("soup3000", 1.05, 0.6)])
+@pytest.mark.parametrize("name,visits,tests", [("sphere5", 0.75, 0.4), ("soup3000", 1.05, 0.6), ("baffle16", 1.1, 1.0)])
 def test_gpu_tree_quality(ctx, name, visits, tests):
     """Traversal work on the GPU-built tree against the reference's tree, as
     the oracle counts it on the same rays (node visits, triangle tests). An

@@ -5,8 +5,8 @@
 // It is not the reference's builder (lib/kdtree.cpp:124-412): the reference
 // sweeps exact event lists sorted with std::sort, whose order among equal
 // keys is that library's and decides the triangle order inside leaves. This
-// build chooses planes among 32 bins per axis for large cells and among all
-// clipped-box bounds for cells of at most kExactMax references, so its tree
+// build chooses planes among 32 bins per axis for cells of more than kMidMax
+// references and among all clipped-box bounds for smaller cells, so its tree
 // differs. Every leaf lists every triangle whose clipped box reaches into the
 // leaf's cell, so closest hits are the same triangles at the same r (checked
 // against a brute-force leaf and the reference's tree in the tests).
@@ -64,6 +64,8 @@ constexpr uint32_t kMaxLevels = 512;                  // breadth-first levels, c
 constexpr uint32_t kExactMax = 1024;                  // cells this small sweep every box bound
 constexpr uint32_t kSmallMax = 32;                    // cells this small take one warp instead of a block
 constexpr int kSmallWarps = 8;                        // warps (cells) per block of k_level_small
+constexpr uint32_t kMidMax = 8192;                     // cells up to this size (above kExactMax) sort their bounds
+constexpr int kMidThreads = 512;
 constexpr float kCostTraversal = 15.f, kCostIntersection = 20.f;
 
 struct Cell {
@@ -408,6 +410,189 @@ __global__ void __launch_bounds__(kLevelThreads) k_level(const Cell* __restrict_
     }
 }
 
+// Number of a[0..n) below x (lower bound) and not above x (upper bound) in
+// an ascending array.
+__device__ __forceinline__ uint32_t count_below(const float* a, uint32_t n, float x) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t m = (lo + hi) >> 1;
+        if (a[m] < x) lo = m + 1;
+        else hi = m;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t count_not_above(const float* a, uint32_t n, float x) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t m = (lo + hi) >> 1;
+        if (a[m] <= x) lo = m + 1;
+        else hi = m;
+    }
+    return lo;
+}
+
+// Ascending bitonic sort of three shared arrays of length len (a power of
+// two) at once, by all threads of the block.
+__device__ void bitonic_sort3(float* a, float* b, float* c, uint32_t len) {
+    for (uint32_t k = 2; k <= len; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const bool up = (i & k) == 0;
+                    float x = a[i], y = a[ixj];
+                    if ((x > y) == up) { a[i] = y; a[ixj] = x; }
+                    x = b[i]; y = b[ixj];
+                    if ((x > y) == up) { b[i] = y; b[ixj] = x; }
+                    x = c[i]; y = c[ixj];
+                    if ((x > y) == up) { c[i] = y; c[ixj] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One block per listed cell of kExactMax + 1 .. kMidMax references: the exact
+// sweep of k_level (every clipped-box bound is a candidate, with the same
+// counts, choice and termination test), but each axis sorts its kept boxes'
+// lower bounds, upper bounds and flat positions in shared memory and counts by
+// binary search, O(n log^2 n) instead of O(n^2). The clipped boxes go through
+// `boxes` (6 floats per reference, an empty box for one that misses the cell).
+__global__ void __launch_bounds__(kMidThreads) k_level_mid(const Cell* __restrict__ cells,
+                                                           const uint32_t* __restrict__ list,
+                                                           const uint32_t* __restrict__ refs,
+                                                           const float* __restrict__ verts,
+                                                           const float* __restrict__ tri_box, bool last_level,
+                                                           Decision* __restrict__ dec, uint64_t* __restrict__ flags,
+                                                           float* __restrict__ boxes) {
+    extern __shared__ float mid_smem[];
+    float* s_lo = mid_smem;
+    float* s_hi = s_lo + kMidMax;
+    float* s_pl = s_hi + kMidMax;
+    float* r_cost = s_pl + kMidMax;
+    float* r_pos = r_cost + kMidThreads;
+    int* r_axis = reinterpret_cast<int*>(r_pos + kMidThreads);
+    int* r_pl = r_axis + kMidThreads;
+    uint32_t* r_nl = reinterpret_cast<uint32_t*>(r_pl + kMidThreads);
+    uint32_t* r_nr = r_nl + kMidThreads;
+    __shared__ uint32_t kept, n_axis, n_pl;
+    __shared__ Decision d;
+    const uint32_t ci = list[blockIdx.x];
+    const Cell c = cells[ci];
+    const int tid = threadIdx.x;
+    if (tid == 0) kept = 0;
+    __syncthreads();
+    for (uint32_t i = tid; i < c.count; i += kMidThreads) {
+        float lo[3], hi[3];
+        float* bx = boxes + 6 * size_t(c.begin + i);
+        if (clip_to(verts, tri_box, refs[c.begin + i], c, lo, hi)) {
+            atomicAdd(&kept, 1u);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                bx[a] = lo[a];
+                bx[3 + a] = hi[a];
+            }
+        } else {
+            bx[0] = INFINITY;   // lower above upper: misses the cell
+            bx[3] = -INFINITY;
+        }
+    }
+    __syncthreads();
+    const uint32_t n = kept;
+    const float sa = surface(c.lo, c.hi);
+    float bc = 3.4e38f, bp = 0.f;
+    int ba = 3, bpl = 0;
+    uint32_t bnl = 0, bnr = 0;
+    if (n > 3 && sa > 0.f) {
+        uint32_t len = 1;
+        while (len < n) len <<= 1;   // n <= c.count <= kMidMax
+        for (int a = 0; a < 3; ++a) {
+            if (tid == 0) {
+                n_axis = 0;
+                n_pl = 0;
+            }
+            __syncthreads();
+            for (uint32_t i = tid; i < c.count; i += kMidThreads) {
+                const float* bx = boxes + 6 * size_t(c.begin + i);
+                if (!(bx[0] <= bx[3])) continue;
+                const float lo = bx[a], hi = bx[3 + a];
+                const uint32_t j = atomicAdd(&n_axis, 1u);
+                s_lo[j] = lo;
+                s_hi[j] = hi;
+                if (lo == hi) s_pl[atomicAdd(&n_pl, 1u)] = lo;
+            }
+            __syncthreads();
+            const uint32_t npl = n_pl;
+            for (uint32_t i = n + tid; i < len; i += kMidThreads) {
+                s_lo[i] = INFINITY;
+                s_hi[i] = INFINITY;
+            }
+            for (uint32_t i = npl + tid; i < len; i += kMidThreads) s_pl[i] = INFINITY;
+            __syncthreads();
+            bitonic_sort3(s_lo, s_hi, s_pl, len);
+            for (uint32_t t = tid; t < 2 * n; t += kMidThreads) {
+                const float pos = t < n ? s_lo[t] : s_hi[t - n];
+                if (!(pos >= c.lo[a] && pos <= c.hi[a])) continue;
+                const uint32_t nl = count_below(s_lo, n, pos);
+                const uint32_t nr = n - count_not_above(s_hi, n, pos);
+                const uint32_t np = count_not_above(s_pl, npl, pos) - count_below(s_pl, npl, pos);
+                consider(c, sa, n, a, pos, nl, nr, np, bc, ba, bp, bpl, bnl, bnr);
+            }
+            __syncthreads();   // the next axis refills the arrays
+        }
+    }
+    r_cost[tid] = bc;
+    r_axis[tid] = ba;
+    r_pos[tid] = bp;
+    r_pl[tid] = bpl;
+    r_nl[tid] = bnl;
+    r_nr[tid] = bnr;
+    __syncthreads();
+    for (int h = kMidThreads / 2; h > 0; h >>= 1) {
+        if (tid < h && better(r_cost[tid + h], r_axis[tid + h], r_pos[tid + h], r_pl[tid + h], r_cost[tid], r_axis[tid],
+                              r_pos[tid], r_pl[tid])) {
+            r_cost[tid] = r_cost[tid + h];
+            r_axis[tid] = r_axis[tid + h];
+            r_pos[tid] = r_pos[tid + h];
+            r_pl[tid] = r_pl[tid + h];
+            r_nl[tid] = r_nl[tid + h];
+            r_nr[tid] = r_nr[tid + h];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        Decision r{0, 0, 0.f, n, 1};
+        if (n > 3 && c.depth < kMaxBuildDepth && !last_level && r_axis[0] < 3) {
+            if (!(kCostIntersection * static_cast<float>(n) < r_cost[0])) {   // the termination test of k_level
+                r.split = 1;
+                r.axis = r_axis[0];
+                r.pos = r_pos[0];
+                r.planar_left = r_pl[0];
+            }
+        }
+        d = r;
+        dec[ci] = r;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < c.count; i += kMidThreads) {
+        const float* bx = boxes + 6 * size_t(c.begin + i);
+        uint64_t f = 0;
+        if (bx[0] <= bx[3]) {
+            if (!d.split) {
+                f = 1;
+            } else {
+                const bool pl = d.planar_left != 0;
+                const bool gl = goes_left(bx[d.axis], bx[3 + d.axis], d.pos, pl);
+                const bool gr = goes_right(bx[d.axis], bx[3 + d.axis], d.pos, pl);
+                f = (gl ? 1ull : 0ull) | (gr ? (1ull << 32) : 0ull);
+            }
+        }
+        flags[c.begin + i] = f;
+    }
+}
+constexpr size_t kMidSmem = sizeof(float) * 3 * kMidMax + sizeof(float) * 6 * kMidThreads;
+
 // One warp per listed cell of at most kSmallMax references (one reference per
 // lane): the same clipping, exact candidate sweep, choice and termination test
 // as k_level, without its block-wide histograms and reductions. Deep levels
@@ -591,7 +776,7 @@ struct Arena {
 // Arena slots. A scan at recursion depth k uses kSlotScan + 2k and + 2k + 1.
 enum : size_t {
     kSlotVerts, kSlotBoxes, kSlotCells0, kSlotCells1, kSlotRefs0, kSlotRefs1, kSlotRefCell0, kSlotRefCell1,
-    kSlotSmall0, kSlotSmall1, kSlotLarge0, kSlotLarge1, kSlotDec, kSlotFlags, kSlotFscan, kSlotNChild, kSlotNNext,
+    kSlotSmall0, kSlotSmall1, kSlotLarge0, kSlotLarge1, kSlotMid0, kSlotMid1, kSlotBoxes6, kSlotDec, kSlotFlags, kSlotFscan, kSlotNChild, kSlotNNext,
     kSlotNLeaf, kSlotChildBase, kSlotNextBase, kSlotLeafBase, kSlotLeafPool, kSlotLevelNodes, kSlotLists, kSlotScan
 };
 
@@ -655,15 +840,16 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n) 
 }
 
 // The next level's cells and BFS records of this level's nodes; the children
-// are also listed by size for the next level's two kernels (lists[0] counts
-// and small_list holds cells of at most kSmallMax references, lists[1] and
-// large_list the others).
+// are also listed by size for the next level's three kernels: lists[0] counts
+// and small_list holds cells of at most kSmallMax references, lists[2] and
+// mid_list those of kExactMax + 1 .. kMidMax, lists[1] and large_list the
+// others.
 __global__ void k_children(const Cell* __restrict__ cells, const Decision* __restrict__ dec,
                            const uint64_t* __restrict__ fscan, uint32_t n, const uint32_t* __restrict__ child_base,
                            const uint32_t* __restrict__ next_base, const uint32_t* __restrict__ leaf_base,
                            uint32_t leaf_offset, int32_t next_level_offset, Cell* __restrict__ next_cells,
                            BfsNode* __restrict__ out, uint32_t* __restrict__ lists, uint32_t* __restrict__ small_list,
-                           uint32_t* __restrict__ large_list) {
+                           uint32_t* __restrict__ large_list, uint32_t* __restrict__ mid_list) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     // every lane takes part in the list appends; lanes past n add nothing
     uint32_t child[2] = {0, 0}, count[2] = {0, 0};
@@ -707,12 +893,17 @@ __global__ void k_children(const Cell* __restrict__ cells, const Decision* __res
     }
     out[i] = r;
     }
-    uint32_t n_small = 0;
-    for (uint32_t k = 0; k < n_children; ++k) n_small += count[k] <= kSmallMax ? 1u : 0u;
+    uint32_t n_small = 0, n_mid = 0;
+    for (uint32_t k = 0; k < n_children; ++k) {
+        n_small += count[k] <= kSmallMax ? 1u : 0u;
+        n_mid += (count[k] > kExactMax && count[k] <= kMidMax) ? 1u : 0u;
+    }
     uint32_t small_at = warp_reserve(lists, n_small);
-    uint32_t large_at = warp_reserve(lists + 1, n_children - n_small);
+    uint32_t large_at = warp_reserve(lists + 1, n_children - n_small - n_mid);
+    uint32_t mid_at = warp_reserve(lists + 2, n_mid);
     for (uint32_t k = 0; k < n_children; ++k) {
         if (count[k] <= kSmallMax) small_list[small_at++] = child[k];
+        else if (count[k] > kExactMax && count[k] <= kMidMax) mid_list[mid_at++] = child[k];
         else large_list[large_at++] = child[k];
     }
 }
@@ -923,14 +1114,19 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
     root.depth = 0;
     uint32_t n_cells = 1, n_refs = n_tris;
     // the root is the only cell of level 0, in the small or the large list
-    uint32_t n_small = n_tris <= kSmallMax ? 1u : 0u, n_large = 1u - n_small;
+    uint32_t n_small = n_tris <= kSmallMax ? 1u : 0u;
+    uint32_t n_mid = (n_tris > kExactMax && n_tris <= kMidMax) ? 1u : 0u;
+    uint32_t n_large = 1u - n_small - n_mid;
     Cell* cells = nullptr;
-    uint32_t *refs = nullptr, *ref_cell = nullptr, *small_list = nullptr, *large_list = nullptr;
+    uint32_t *refs = nullptr, *ref_cell = nullptr, *small_list = nullptr, *large_list = nullptr, *mid_list = nullptr;
     GB_CK(arena.get(kSlotCells0, &cells, 1));
     GB_CK(arena.get(kSlotRefs0, &refs, n_refs));
     GB_CK(arena.get(kSlotRefCell0, &ref_cell, n_refs));
     GB_CK(arena.get(kSlotSmall0, &small_list, 1));
     GB_CK(arena.get(kSlotLarge0, &large_list, 1));
+    GB_CK(arena.get(kSlotMid0, &mid_list, 1));
+    GB_CK(cudaMemsetAsync(mid_list, 0, sizeof(uint32_t), st));
+    GB_CK(cudaFuncSetAttribute(k_level_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kMidSmem)));
     GB_CK(cudaMemcpyAsync(cells, &root, sizeof(Cell), cudaMemcpyHostToDevice, st));
     GB_CK(cudaMemsetAsync(small_list, 0, sizeof(uint32_t), st));
     GB_CK(cudaMemsetAsync(large_list, 0, sizeof(uint32_t), st));
@@ -961,7 +1157,7 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         GB_CK(arena.get(kSlotChildBase, &child_base, size_t(n_cells) + 1));
         GB_CK(arena.get(kSlotNextBase, &next_base, size_t(n_cells) + 1));
         GB_CK(arena.get(kSlotLeafBase, &leaf_base, size_t(n_cells) + 1));
-        GB_CK(arena.get(kSlotLists, &lists, 2));
+        GB_CK(arena.get(kSlotLists, &lists, 3));
         const bool last = level + 1 >= kMaxLevels;
         if (n_large) {
             k_level<<<n_large, kLevelThreads, 0, st>>>(cells, large_list, refs, d_v, d_box, last, dec, flags);
@@ -969,6 +1165,12 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         if (n_small) {
             k_level_small<<<(n_small + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, 0, st>>>(
                 cells, small_list, n_small, refs, d_v, d_box, last, dec, flags);
+        }
+        if (n_mid) {
+            float* boxes6 = nullptr;
+            GB_CK(arena.get(kSlotBoxes6, &boxes6, 6 * size_t(n_refs)));
+            k_level_mid<<<n_mid, kMidThreads, kMidSmem, st>>>(cells, mid_list, refs, d_v, d_box, last, dec, flags,
+                                                              boxes6);
         }
         GB_CK(cudaGetLastError());
         GB_CK(scan_exclusive<uint64_t>(flags, n_refs, fscan, st, arena));
@@ -988,19 +1190,20 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
 
         Cell* next_cells = nullptr;
         uint32_t *next_refs = nullptr, *next_ref_cell = nullptr, *next_small = nullptr, *next_large = nullptr,
-                 *leaf_pool = nullptr;
+                 *next_mid = nullptr, *leaf_pool = nullptr;
         BfsNode* level_nodes = nullptr;
         GB_CK(arena.get(kSlotCells0 + nxt, &next_cells, next_cells_n));
         GB_CK(arena.get(kSlotRefs0 + nxt, &next_refs, next_refs_n));
         GB_CK(arena.get(kSlotRefCell0 + nxt, &next_ref_cell, next_refs_n));
         GB_CK(arena.get(kSlotSmall0 + nxt, &next_small, next_cells_n));
         GB_CK(arena.get(kSlotLarge0 + nxt, &next_large, next_cells_n));
+        GB_CK(arena.get(kSlotMid0 + nxt, &next_mid, next_cells_n));
         GB_CK(arena.get(kSlotLeafPool, &leaf_pool, leaf_n));
         GB_CK(arena.get(kSlotLevelNodes, &level_nodes, n_cells));
-        GB_CK(cudaMemsetAsync(lists, 0, 2 * sizeof(uint32_t), st));
+        GB_CK(cudaMemsetAsync(lists, 0, 3 * sizeof(uint32_t), st));
         const int32_t next_offset = static_cast<int32_t>(bfs.size() + n_cells);
         k_children<<<gc, 256, 0, st>>>(cells, dec, fscan, n_cells, child_base, next_base, leaf_base, leaf_total,
-                                       next_offset, next_cells, level_nodes, lists, next_small, next_large);
+                                       next_offset, next_cells, level_nodes, lists, next_small, next_large, next_mid);
         if (n_refs) {
             k_scatter<<<(n_refs + 255) / 256, 256, 0, st>>>(cells, dec, refs, ref_cell, flags, fscan, n_refs,
                                                             child_base, next_base, leaf_base, next_refs,
@@ -1014,7 +1217,7 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         } catch (const std::bad_alloc&) {
             return TURNER_ERR_OUT_OF_MEMORY;
         }
-        uint32_t counts[2] = {0, 0};
+        uint32_t counts[3] = {0, 0, 0};
         GB_CK(cudaMemcpyAsync(bfs.data() + base, level_nodes, sizeof(BfsNode) * n_cells, cudaMemcpyDeviceToHost, st));
         if (leaf_n)
             GB_CK(cudaMemcpyAsync(pool.data() + leaf_total, leaf_pool, sizeof(uint32_t) * leaf_n,
@@ -1028,11 +1231,13 @@ int turner_kdtree_build_gpu(turner_ctx* ctx, const float* vertices, const float*
         ref_cell = next_ref_cell;
         small_list = next_small;
         large_list = next_large;
+        mid_list = next_mid;
         n_cells = next_cells_n;
         n_refs = next_refs_n;
         n_small = counts[0];
         n_large = counts[1];
-        if (n_small + n_large != n_cells) return TURNER_ERR_CUDA;
+        n_mid = counts[2];
+        if (n_small + n_large + n_mid != n_cells) return TURNER_ERR_CUDA;
     }
 #undef GB_CK
     int status;
