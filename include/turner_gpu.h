@@ -388,8 +388,8 @@ int turner_kdtree_set_reflective(turner_kdtree* tree, const float* reflective);
 
 /* Builds a kd-tree on the context's GPU, level by level: SAH with the
  * reference's cost constants and termination test over 32 bins per axis in
- * large cells and over every clipped-box bound in cells of at most 1024
- * triangles, triangles classified by their polygons clipped to each cell,
+ * cells of more than 8192 triangles and over every clipped-box bound in
+ * smaller cells, triangles classified by their polygons clipped to each cell,
  * and no empty-space splits (the flattened tree could not keep them). No counterpart
  * for the build itself: the reference builds on the host
  * (lib/kdtree.cpp:124-412), and its node words depend on std::sort's order
