@@ -137,6 +137,15 @@ typedef struct turner_job {
     int32_t renderer;             /* TURNER_RENDERER_*: which trace() plug-in */
     float shadow_intensity;       /* raytracer --shadow (config.h: 0.5)       */
     float max_visibility;         /* raycaster --max-visibility (config.h: 2) */
+    /* Image rows [row_begin, row_end) to render; row_end = 0 means height.
+     * The reference's unit of work is one image row (main.cpp:193-226); a
+     * band is what one GPU of a row-partitioned frame renders. The camera
+     * and every (pixel, sample) stream use the pixel's place in the whole
+     * image, so a band is bit-identical to the same rows of a full render.
+     * The output then holds only the band: width * (row_end - row_begin)
+     * pixels, its first row being row_begin. */
+    uint32_t row_begin;
+    uint32_t row_end;
 } turner_job;
 
 /* The reference links one trace() per executable (trace.h:23-25):
@@ -190,6 +199,15 @@ int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths);
  * one thread per ray. No reference counterpart: tuning knob of this library. */
 int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks_per_sm);
 
+/* Gather-bandwidth roof of the traversal: times a kernel that makes
+ * independent loads of load_bytes (8: one node word; 32: one half of a
+ * triangle record) at random positions in a buffer of buffer_bytes (a power
+ * of two, at least 4096; 64 MiB fits in L2 as the large-mesh scene does),
+ * best of `repeats` launches after a warm-up launch, CUDA events; *gbs =
+ * bytes loaded / time. Allocates and frees its buffer. No reference
+ * counterpart: the roof against which traversal throughput is reported. */
+int turner_probe_gather(turner_ctx* ctx, uint64_t buffer_bytes, uint32_t load_bytes, uint32_t repeats, double* gbs);
+
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the
  * reference only has Runtime wall-clock timers (lib/runtime.h). */
@@ -234,6 +252,20 @@ int turner_validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tr
 int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
                      const float* dx, const float* dy, const float* dz, uint64_t n, uint32_t* hit_id, float* r,
                      float* s, float* t, int mode, uint32_t flags);
+
+/* Batched shadow-ray test of the path tracer (pathtracer.cpp:44-58): the
+ * reference traces the closest hit from p2 toward the light and calls the
+ * point lit when there is no hit or r_closest > |light - p2|. Here
+ * blocked[i] = 1 iff the ray (SoA as in turner_intersect) has a valid
+ * triangle intersection with r <= tmax[i] in a leaf its traversal visits,
+ * else 0: the same predicate, so blocked == !(miss || r_closest > tmax)
+ * for the reference's closest hit, decided without finding the closest hit
+ * (traversal stops at the first such triangle). The renders use the same
+ * test for their shadow rays. `flags` selects host or device buffers.
+ * Synchronous. */
+int turner_occluded(turner_ctx* ctx, uint32_t scene_id, const float* ox, const float* oy, const float* oz,
+                    const float* dx, const float* dy, const float* dz, const float* tmax, uint64_t n,
+                    uint8_t* blocked, uint32_t flags);
 
 /* Batched intersect that allocates nothing. No counterpart in the reference.
  * For callers that must not allocate device memory while they run: a

@@ -41,3 +41,17 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+@pytest.fixture(scope="session")
+def sphere_room_327k():
+    """The large-mesh workload's scene: the 327,692-triangle displaced sphere
+    room (icosphere subdivided 7 times), its host kd-tree (the reference
+    builder's node words) and the oracle on that tree. Built once per session."""
+    import turner_gb300 as tg
+
+    from oracle import oracle as orc
+
+    mesh = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=7, aspect=16 / 9)
+    nodes, tris, box = tg.KDTree.from_mesh(mesh).export()
+    return mesh, nodes, tris, box, orc.Scene(nodes, tris, box)

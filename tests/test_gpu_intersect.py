@@ -209,14 +209,11 @@ def test_bad_scene_rejected(ctx):
 
 
 @pytest.mark.slow
-def test_full_hit_test_set(ctx):
+def test_full_hit_test_set(ctx, sphere_room_327k):
     """16,777,216 rays (origins uniform in the room, directions uniform on the
     sphere) against the 327,692-triangle tree: every hit index equal."""
-    m = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=7, aspect=16 / 9)
-    t = tg.KDTree.from_mesh(m)
-    nodes, tris, box = t.export()
+    _, nodes, tris, box, ref = sphere_room_327k
     sid = ctx.upload(nodes, tris, box)
-    ref = orc.Scene(nodes, tris, box)
     n = 1 << 24
     o, d = tg.make_rays(n, box, seed=2024)
     gpu = ctx.intersect(sid, o, d)

@@ -80,7 +80,12 @@ class Job(C.Structure):
                 ("background", C.c_float * 3), ("seed", C.c_uint64), ("n_lights", C.c_int32),
                 ("light", Light), ("camera", Camera), ("sampling", C.c_int32), ("traversal", C.c_int32),
                 ("linear_output", C.c_int32), ("renderer", C.c_int32), ("shadow_intensity", C.c_float),
-                ("max_visibility", C.c_float)]
+                ("max_visibility", C.c_float), ("row_begin", C.c_uint32), ("row_end", C.c_uint32)]
+
+    @property
+    def rows(self) -> int:
+        """Rows this job renders (its output's height): [row_begin, row_end)."""
+        return (self.row_end or self.height) - self.row_begin
 
 
 class Tuning(C.Structure):
@@ -129,6 +134,8 @@ def _lib() -> C.CDLL:
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
         "turner_validate_nodes": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]),
         "turner_intersect": (C.c_int, [_P, C.c_uint32] + [_P] * 6 + [C.c_uint64] + [_P] * 4 + [C.c_int, C.c_uint32]),
+        "turner_probe_gather": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]),
+        "turner_occluded": (C.c_int, [_P, C.c_uint32] + [_P] * 7 + [C.c_uint64, _P, C.c_uint32]),
         "turner_intersect_noalloc": (C.c_int, [_P, C.c_uint32] + [_P] * 6 + [C.c_uint64] + [_P] * 4 + [C.c_int]),
         "turner_render": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.POINTER(_P), C.POINTER(Stats), C.c_uint32]),
         "turner_render_accumulate": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, _P, C.POINTER(C.c_uint64),
@@ -406,6 +413,14 @@ class Context:
         _check(_lib().turner_set_traversal_launch(self._h, 1 if persistent else 0, blocks_per_sm),
                "turner_set_traversal_launch")
 
+    def probe_gather(self, buffer_bytes: int = 64 << 20, load_bytes: int = 8, repeats: int = 5) -> float:
+        """GB/s of independent random loads of load_bytes over a buffer of
+        buffer_bytes (the traversal's gather roof when the buffer fits L2)."""
+        v = C.c_double()
+        _check(_lib().turner_probe_gather(self._h, buffer_bytes, load_bytes, repeats, C.byref(v)),
+               "turner_probe_gather")
+        return v.value
+
     def set_profiling(self, on: bool) -> None:
         _check(_lib().turner_set_profiling(self._h, 1 if on else 0), "turner_set_profiling")
 
@@ -446,6 +461,20 @@ class Context:
                                        _ptr(d[2]), n, _ptr(hid), _ptr(r), _ptr(s), _ptr(t), mode, HOST_BUFFERS),
                "turner_intersect")
         return hid, r, s, t
+
+    def occluded(self, scene_id: int, o: np.ndarray, d: np.ndarray, tmax: np.ndarray) -> np.ndarray:
+        """Host-buffer shadow-ray test: o, d (3, n), tmax (n,) float32. Returns
+        blocked (n,) bool: some valid intersection with r <= tmax
+        (pathtracer.cpp:44-58: lit iff no hit or r_closest > distance)."""
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        tm = np.ascontiguousarray(tmax, np.float32).reshape(-1)
+        n = o.shape[1]
+        assert tm.size == n
+        out = np.empty(n, np.uint8)
+        _check(_lib().turner_occluded(self._h, scene_id, _ptr(o[0]), _ptr(o[1]), _ptr(o[2]), _ptr(d[0]), _ptr(d[1]),
+                                      _ptr(d[2]), _ptr(tm), n, _ptr(out), HOST_BUFFERS), "turner_occluded")
+        return out.astype(bool)
 
     def intersect_device(self, scene_id: int, ptrs: list[int], n: int, out_ptrs: list[int],
                          mode: int = TRAVERSAL_PARITY) -> None:
@@ -492,7 +521,7 @@ class Context:
     def accumulate(self, job: Job, passes: int) -> tuple[np.ndarray, int]:
         """FP64 running mean of linear radiance after `passes` more passes of
         job.pixel_samples samples each: ((h, w, 4) float64, total samples)."""
-        out = np.empty((job.height, job.width, 4), np.float64)
+        out = np.empty((max(0, job.rows), job.width, 4), np.float64)
         total = C.c_uint64(0)
         _check(_lib().turner_render_accumulate(self._h, C.byref(job), passes, _ptr(out), C.byref(total),
                                                HOST_BUFFERS), "turner_render_accumulate")
@@ -505,7 +534,8 @@ class Context:
         stats = (Stats * len(jobs))()
         images = None
         if flags == HOST_BUFFERS:
-            images = [np.empty((j.height, j.width, 4), np.float32) for j in jobs]
+            # a bad row range is the library's to refuse: no negative shapes here
+            images = [np.empty((max(0, j.rows), j.width, 4), np.float32) for j in jobs]
             outs = [_ptr(im) for im in images]
         ptrs = (_P * len(jobs))(*outs)
         _check(_lib().turner_render(self._h, arr, len(jobs), ptrs, stats, flags), "turner_render")
@@ -596,9 +626,11 @@ def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, p
              max_depth: int = 3, monte_carlo_samples: int = 1, seed: int = 1, exposure: float = 1.0,
              inverse_gamma: float = 0.454545, gamma_correction: bool = True, background=(0.0, 0.0, 0.0),
              sampling: int = SAMPLING_UNIFORM, traversal: int = TRAVERSAL_PARITY, renderer: int = RENDERER_PATH,
-             shadow_intensity: float = 0.5, max_visibility: float = 2.0) -> Job:
+             shadow_intensity: float = 0.5, max_visibility: float = 2.0,
+             rows: tuple[int, int] | None = None) -> Job:
     """A job with the reference's defaults (config.h, pathtracer.h,
-    raytracer.h, raycaster.h)."""
+    raytracer.h, raycaster.h). rows=(y0, y1) renders only image rows
+    [y0, y1) (the reference's unit of work is one row, main.cpp:193-226)."""
     j = Job()
     j.scene_id = scene_id
     j.width = width
@@ -621,6 +653,8 @@ def make_job(scene_id: int, mesh: Mesh, width: int, height: int | None = None, p
     j.renderer = renderer
     j.shadow_intensity = shadow_intensity
     j.max_visibility = max_visibility
+    if rows is not None:
+        j.row_begin, j.row_end = int(rows[0]), int(rows[1])
     return j
 
 

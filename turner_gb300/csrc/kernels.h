@@ -63,7 +63,8 @@ struct JobDesc {
     float cam_pos[3];
     float trafo[9];
     float delta_x, delta_y;
-    uint32_t width, height, spp;
+    uint32_t width, height, spp;   // height: the whole image's (the camera's raster)
+    uint32_t row0, rows;           // the band rendered: rows [row0, row0 + rows)
     int32_t max_depth, mc;
     float bg[3];
     uint64_t seed;
@@ -107,6 +108,20 @@ struct TraverseCfg {
 void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                       const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
                       int fast, const TraverseCfg& cfg, cudaStream_t stream);
+
+// Any-hit occlusion of SoA rays: blocked[i] = 1 iff some triangle of a leaf the
+// ray's traversal visits has a valid intersection with r <= tmax[i]. Persistent
+// launch; cfg.work must be a zeroed device counter.
+void launch_occluded(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
+                     const float* dy, const float* dz, const float* tmax, uint32_t n, uint8_t* blocked,
+                     const TraverseCfg& cfg, cudaStream_t stream);
+
+// Gather-bandwidth probe: blocks x 256 threads, each making loads_per_thread
+// (a multiple of 8) independent loads of load_bytes (8 or 32) at random
+// positions in buf (buf_bytes / load_bytes a power of two, buf 32-byte
+// aligned); out receives one word per thread.
+void launch_gather_probe(const void* buf, uint64_t buf_bytes, int load_bytes, uint32_t loads_per_thread,
+                         uint32_t seed, uint32_t* out, unsigned blocks, cudaStream_t stream);
 
 // `single` is the scene of every job when the batch has one scene (rays then
 // skip the per-ray job-table lookup); nullptr for multi-scene batches.

@@ -118,8 +118,11 @@ __global__ void __launch_bounds__(kBlock) k_camera(const JobDesc* __restrict__ j
     const uint32_t j = job_of_path(jobs, n_jobs, g);
     const JobDesc& job = jobs[j];
     const uint64_t local = g - job.path_offset;
-    const uint64_t pixel = local / job.spp;
-    const uint32_t sample = static_cast<uint32_t>(local - pixel * job.spp);
+    const uint64_t band_pixel = local / job.spp;
+    const uint32_t sample = static_cast<uint32_t>(local - band_pixel * job.spp);
+    // the pixel's index in the whole image: a band of rows draws the same
+    // streams and rays as those rows of a full render
+    const uint64_t pixel = uint64_t(job.row0) * job.width + band_pixel;
     const uint32_t y = static_cast<uint32_t>(pixel / job.width);
     const uint32_t x = static_cast<uint32_t>(pixel - uint64_t(y) * job.width);
     uint64_t js, bs;
@@ -646,6 +649,20 @@ struct SoaSrc {             // turner_intersect batches
     }
 };
 
+struct OccSrc {             // turner_occluded batches: any hit with r <= tmax[i]
+    const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;
+    uint32_t n;
+    uint8_t* blocked;
+    __device__ uint32_t count() const { return n; }
+    __device__ void load(uint32_t i, float3& o3, float3& d3, float& tm, uint32_t& job) const {
+        o3 = make_float3(ox[i], oy[i], oz[i]);
+        d3 = make_float3(dx[i], dy[i], dz[i]);
+        tm = tmax[i];
+        job = 0;
+    }
+    __device__ void store(uint32_t i, const Hit& h) const { blocked[i] = h.id < kMiss ? 1 : 0; }
+};
+
 // Persistent traversal: each lane holds one ray; lanes whose ray is finished
 // take the next unclaimed ray (one atomicAdd per warp), so warps stay full
 // while rays of very different lengths are traversed. MULTI: every ray names
@@ -857,7 +874,48 @@ __global__ void __launch_bounds__(kBlock) k_shadow_flat(SceneView single, const 
     }
 }
 
+// Gather-bandwidth probe: every thread makes `loads` independent loads of
+// BYTES (8: one kd-tree node word; 32: one half of a triangle record, the
+// traversal's 256-bit load) at pseudo-random positions in a buffer of
+// n_units such units (a power of two), so nearly every load misses L1 and is
+// served by L2 when the buffer fits there. Eight loads are in flight per
+// thread, as in a warp of independent rays; the XOR of what was read is
+// stored so that no load is removed.
+template <int BYTES>
+__global__ void __launch_bounds__(256) k_gather_probe(const float4* __restrict__ buf, uint32_t mask, uint32_t loads,
+                                                      uint32_t seed, uint32_t* __restrict__ out) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = static_cast<uint32_t>(splitmix64(uint64_t(tid) * 8 + j + (uint64_t(seed) << 40)));
+    uint32_t acc = 0;
+    for (uint32_t k = 0; k < loads; k += 8) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t u = x[j] & mask;
+            if (BYTES == 8) {
+                const uint2 w = __ldg(reinterpret_cast<const uint2*>(buf) + u);
+                acc ^= w.x ^ w.y;
+            } else {
+                float4 a, b;
+                ldg_pair(buf + 2 * size_t(u), a, b);
+                acc ^= __float_as_uint(a.x) ^ __float_as_uint(a.w) ^ __float_as_uint(b.y) ^ __float_as_uint(b.z);
+            }
+            x[j] = x[j] * 1664525u + 1013904223u;
+        }
+    }
+    out[tid] = acc;
+}
+
 } // namespace
+
+void launch_gather_probe(const void* buf, uint64_t buf_bytes, int load_bytes, uint32_t loads_per_thread,
+                         uint32_t seed, uint32_t* out, unsigned blocks, cudaStream_t stream) {
+    const uint32_t mask = static_cast<uint32_t>(buf_bytes / static_cast<uint64_t>(load_bytes) - 1);
+    const float4* b = static_cast<const float4*>(buf);
+    if (load_bytes == 8) k_gather_probe<8><<<blocks, 256, 0, stream>>>(b, mask, loads_per_thread, seed, out);
+    else k_gather_probe<32><<<blocks, 256, 0, stream>>>(b, mask, loads_per_thread, seed, out);
+}
 
 void launch_intersect(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
                       const float* dy, const float* dz, uint64_t n, uint32_t* id, float* r, float* s, float* t,
@@ -870,6 +928,15 @@ void launch_intersect(const SceneView& sc, const float* ox, const float* oy, con
         return;
     }
     k_intersect<<<grid_for(n), kBlock, 0, stream>>>(sc, ox, oy, oz, dx, dy, dz, n, id, r, s, t, fast);
+}
+
+void launch_occluded(const SceneView& sc, const float* ox, const float* oy, const float* oz, const float* dx,
+                     const float* dy, const float* dz, const float* tmax, uint32_t n, uint8_t* blocked,
+                     const TraverseCfg& cfg, cudaStream_t stream) {
+    if (n == 0) return;
+    // the shadow kernels' default shape: persistent 128-thread blocks, registers capped for 10 per SM
+    const OccSrc src{ox, oy, oz, dx, dy, dz, tmax, n, blocked};
+    run_traverse_shape<OccSrc, true, false, false, 128, kStackCap, false, 10>(sc, nullptr, src, n, cfg, stream);
 }
 
 void launch_camera(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, const RayQueue& q, float4* L,
