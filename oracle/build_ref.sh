@@ -6,9 +6,13 @@
 # third-party dependencies (assimp, cereal, docopt, ThreadPool) are absent.
 #
 # Flags follow the parity contract: -O2 -ffp-contract=off, no -march.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT
 set -euo pipefail
-REF="${1:-/root/reference}"
+if [ $# -lt 1 ]; then
+    echo "usage: $0 REFERENCE_ROOT (the reference's source tree)" >&2
+    exit 2
+fi
+REF="$1"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/lib/kdtree.cpp" ]; then

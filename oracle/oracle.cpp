@@ -552,11 +552,13 @@ void orc_intersect(void* s, const float* rays, uint64_t n, uint32_t* id, float* 
 }
 
 // Render (main.cpp:181-236 with harness seeding). out_rgba: width*height*4.
-// rows [row_begin, row_end) only (row_end = 0 means all rows): bounded CPU
-// samples for the baseline. stats: [rays, primary rays, shadow rays,
+// rows row_begin, row_begin + row_step, ... below row_end only (row_end = 0
+// means all rows, row_step 0 means 1): bounded CPU samples for the baseline,
+// spread over the frame. Threads take one row at a time, as the reference's
+// pool takes one task per row (main.cpp:193-226). stats: [rays, primary rays, shadow rays,
 // node visits and triangle tests of primary/bounce rays, the same of shadow rays].
 void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_rgba, uint64_t* stats,
-                int threads, uint32_t row_begin, uint32_t row_end) {
+                int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step) {
     const Scene& sc = *static_cast<Scene*>(s);
     Conf conf;
     conf.max_depth = p->max_depth;
@@ -579,14 +581,16 @@ void orc_render(void* s, const orc_camera* cam, const orc_params* p, float* out_
     const int spp = static_cast<int>(p->pixel_samples);
     const uint32_t y_end = row_end ? std::min<uint32_t>(row_end, height) : height;
 
-    std::atomic<uint32_t> next_row{row_begin};
+    const uint32_t step = row_step ? row_step : 1;
+    std::atomic<uint32_t> next_row{0};
     std::atomic<uint64_t> n_rays{0}, n_prim{0}, n_shadow{0}, n_visits{0}, n_tests{0}, n_svisits{0}, n_stests{0};
     auto work = [&]() {
         Counters cnt;
         uint64_t prim = 0, visits = 0, tests = 0, svisits = 0, stests = 0;
         for (;;) {
-            const uint32_t y = next_row.fetch_add(1);
-            if (y >= y_end) break;
+            const uint64_t y64 = row_begin + uint64_t(next_row.fetch_add(1)) * step;
+            if (y64 >= y_end) break;
+            const uint32_t y = static_cast<uint32_t>(y64);
             Intersector ti(sc);
             for (int x = 0; x < width; ++x) {
                 C4 acc;

@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "liboracle.so"
+INPUTS_SO = HERE / "libinputs.so"
 REF_SO = HERE / "_ref" / "libturner_ref.so"
 MISS = 0x40000000
 _P = C.c_void_p
@@ -71,7 +72,7 @@ def lib() -> C.CDLL:
         L.orc_scene_free.argtypes = [_P]
         L.orc_intersect.argtypes = [_P, _P, C.c_uint64] + [_P] * 5 + [C.c_int]
         L.orc_render.argtypes = [_P, C.POINTER(OrcCamera), C.POINTER(OrcParams), _P, _P, C.c_int, C.c_uint32,
-                                 C.c_uint32]
+                                 C.c_uint32, C.c_uint32]
         L.orc_write_p3.restype = C.c_uint64
         L.orc_write_p3.argtypes = [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64]
         L.orc_xorshift_floats.argtypes = [C.c_uint64, C.c_uint64, _P]
@@ -81,6 +82,64 @@ def lib() -> C.CDLL:
         L.orc_tone.argtypes = [_P, C.c_uint64, C.c_float, C.c_float, C.c_int, _P]
         _ORC = L
     return _ORC
+
+
+class InputCamera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("trafo", C.c_float * 9), ("delta_x", C.c_float),
+                ("aspect", C.c_float)]
+
+
+class InputLight(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("color", C.c_float * 4)]
+
+
+class SceneInputs:
+    """Input of the CPU reference arm: a seeded synthetic scene and the
+    reference's kd-tree on it (node words identical to KDTree's, pinned by
+    tests/test_builder.py), from oracle/libinputs.so, which holds only the
+    host scene generator and builder (no CUDA). Fields: camera, light (or
+    None), nodes, tris (n, 48), box, n_triangles."""
+
+    def __init__(self, kind: int, detail: int = 0, count: int = 0, seed: int = 1, aspect: float = 1.0):
+        L = C.CDLL(str(INPUTS_SO))
+        L.turner_scene_make.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_uint64, C.c_float, C.POINTER(_P)]
+        L.turner_mesh_num_triangles.restype = C.c_uint32
+        L.turner_mesh_num_triangles.argtypes = [_P]
+        for f in ("turner_mesh_vertices", "turner_mesh_normals", "turner_mesh_diffuse"):
+            getattr(L, f).restype = _P
+            getattr(L, f).argtypes = [_P]
+        L.turner_mesh_camera.argtypes = [_P, C.POINTER(InputCamera), C.POINTER(C.c_float)]
+        L.turner_mesh_light.argtypes = [_P, C.POINTER(InputLight)]
+        L.turner_mesh_free.argtypes = [_P]
+        L.turner_kdtree_build.argtypes = [_P, _P, _P, C.c_uint32, C.c_int, C.POINTER(_P)]
+        L.turner_kdtree_num_nodes.restype = C.c_uint32
+        L.turner_kdtree_num_nodes.argtypes = [_P]
+        L.turner_kdtree_export.argtypes = [_P] * 4
+        L.turner_kdtree_free.argtypes = [_P]
+        mesh = _P()
+        if L.turner_scene_make(kind, detail, count, seed, aspect, C.byref(mesh)) != 0:
+            raise RuntimeError("turner_scene_make failed")
+        try:
+            n = L.turner_mesh_num_triangles(mesh)
+            self.camera = InputCamera()
+            hfov = C.c_float()
+            L.turner_mesh_camera(mesh, C.byref(self.camera), C.byref(hfov))
+            light = InputLight()
+            self.light = light if L.turner_mesh_light(mesh, C.byref(light)) > 0 else None
+            tree = _P()
+            if L.turner_kdtree_build(L.turner_mesh_vertices(mesh), L.turner_mesh_normals(mesh),
+                                     L.turner_mesh_diffuse(mesh), n, 0, C.byref(tree)) != 0:
+                raise RuntimeError("turner_kdtree_build failed")
+        finally:
+            L.turner_mesh_free(mesh)
+        try:
+            self.nodes = np.empty(L.turner_kdtree_num_nodes(tree), np.uint64)
+            self.tris = np.empty((n, 48), np.float32)
+            self.box = np.empty(6, np.float32)
+            L.turner_kdtree_export(tree, _ptr(self.nodes), _ptr(self.tris), _ptr(self.box))
+        finally:
+            L.turner_kdtree_free(tree)
+        self.n_triangles = int(n)
 
 
 def ref_available() -> bool:
@@ -144,10 +203,12 @@ class Scene:
                seed: int = 1, exposure: float = 1.0, inverse_gamma: float = 0.454545, gamma: bool = True,
                background=(0.0, 0.0, 0.0), sampling: int = 0, tone_map: bool = True, threads: int = 0,
                rows: tuple[int, int] | None = None, renderer: int = 0, shadow_intensity: float = 0.5,
-               max_visibility: float = 2.0):
+               max_visibility: float = 2.0, row_step: int = 1):
         """Returns (image (h, w, 4) float32, stats [rays, primary, shadow, closest-hit node visits,
         closest-hit triangle tests, shadow node visits, shadow triangle tests]).
-        renderer: 0 path tracer, 1 Whitted raytracer, 2 raycaster."""
+        renderer: 0 path tracer, 1 Whitted raytracer, 2 raycaster. rows=(a, b)
+        with row_step k renders rows a, a + k, a + 2k, ... below b (the
+        other rows stay zero); threads take one row at a time."""
         cam = OrcCamera()
         cam.position[:] = list(camera.position)
         cam.trafo[:] = list(camera.trafo)
@@ -174,7 +235,7 @@ class Scene:
         stats = np.zeros(7, np.uint64)
         r0, r1 = rows if rows else (0, 0)
         lib().orc_render(self._h, C.byref(cam), C.byref(p), _ptr(img), _ptr(stats), threads or os.cpu_count(),
-                         r0, r1)
+                         r0, r1, row_step)
         return img, stats
 
 

@@ -9,12 +9,23 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parents[1]
 
 
+# runs the reference arm in-process, then reports which native libraries that
+# process mapped: the arm must not load the GPU library
+RUNNER = """
+import runpy, sys
+sys.argv = ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"]
+runpy.run_path("bench.py", run_name="__main__")
+maps = open("/proc/self/maps").read()
+print("MAPPED", int("libturner_gb300" in maps), int("liboracle" in maps))
+"""
+
+
 def test_reference_arm_json_line():
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-                        "--ref-rows", "2"], capture_output=True, text=True, cwd=ROOT, timeout=600)
+    r = subprocess.run([sys.executable, "-c", RUNNER], capture_output=True, text=True, cwd=ROOT, timeout=600)
     assert r.returncode == 0, r.stderr
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
+    assert "MAPPED 0 1" in r.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "Mrays/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1

@@ -4,6 +4,10 @@ Outputs (git-ignored, rebuilt on every machine):
   turner_gb300/lib/libturner_gb300.so   C ABI + sm_103a kernels + host tree/scenes
   turner_gb300/lib/turner_pathtracer     command-line renderer (pathtracer flags)
   oracle/liboracle.so                    CPU oracle (test infrastructure)
+  oracle/libinputs.so                    the host scene generator and kd-tree
+                                         builder alone (no CUDA), which the
+                                         CPU reference arm of bench.py uses to
+                                         make its input
   oracle/_ref/libturner_ref.so           reference checker, only where the
                                          reference sources are present
 
@@ -79,6 +83,10 @@ def build_native(verbose: bool = False) -> Path:
     oracle_cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
                   "-o", str(ORACLE / "liboracle.so"), str(ORACLE / "oracle.cpp"), "-lpthread"]
     cmds.append(oracle_cmd)
+    # the CPU reference arm's input (synthetic scene + the reference's tree)
+    # without the product library and its kernels
+    cmds.append(["g++", *GXX_COMMON, "-shared", "-o", str(ORACLE / "libinputs.so"),
+                 str(CSRC / "host" / "scenes.cpp"), str(CSRC / "host" / "kdtree_build.cpp"), "-lpthread"])
     if verbose:
         for c in cmds:
             print(" ".join(c))
@@ -91,9 +99,16 @@ def build_native(verbose: bool = False) -> Path:
     return so
 
 
+def reference_root() -> Path:
+    """The reference's source tree: $TURNER_REFERENCE, else a checkout named
+    `reference` beside this repository (absent on machines without it)."""
+    env = os.environ.get("TURNER_REFERENCE")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
 def build_reference_checker() -> None:
     """oracle/_ref from the reference's own sources, only where they exist."""
-    ref = Path(os.environ.get("TURNER_REFERENCE", "/root/reference"))
+    ref = reference_root()
     if (ref / "lib" / "kdtree.cpp").exists():
         subprocess.run(["bash", str(ORACLE / "build_ref.sh"), str(ref)], check=True,
                        stdout=subprocess.DEVNULL)
