@@ -208,6 +208,23 @@ int turner_set_traversal_launch(turner_ctx* ctx, int persistent, uint32_t blocks
  * counterpart: the roof against which traversal throughput is reported. */
 int turner_probe_gather(turner_ctx* ctx, uint64_t buffer_bytes, uint32_t load_bytes, uint32_t repeats, double* gbs);
 
+/* Refill threshold of the persistent traversal, per kind of ray: a warp
+ * takes new rays only once `lanes` (1..32) of its 32 lanes are idle. 1
+ * keeps the most lanes busy; 32 takes rays a whole warp at a time, so that
+ * neighbouring rays of a coherent queue stay in one warp and share their
+ * node and triangle loads. Defaults: 32 for camera rays and their shadow
+ * rays (a warp holds 32 samples of neighbouring pixels), 2 for bounce rays,
+ * 4 for their shadow rays, 1 for turner_intersect / turner_occluded.
+ * Results do not depend on it. No reference counterpart: tuning knob of
+ * this library. */
+#define TURNER_RAYS_PRIMARY 0         /* camera rays (depth 0)                  */
+#define TURNER_RAYS_BOUNCE 1          /* bounce rays (depth >= 1)               */
+#define TURNER_RAYS_SHADOW_PRIMARY 2  /* shadow rays from camera-ray hits       */
+#define TURNER_RAYS_SHADOW 3          /* shadow rays from bounce-ray hits       */
+#define TURNER_RAYS_INTERSECT 4       /* turner_intersect and turner_occluded   */
+#define TURNER_RAYS_KINDS 5
+int turner_set_traversal_refill(turner_ctx* ctx, int kind, uint32_t lanes);
+
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the
  * reference only has Runtime wall-clock timers (lib/runtime.h). */

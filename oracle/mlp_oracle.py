@@ -13,8 +13,8 @@ against the GPU kernels (tests/test_gpu_guide.py).
           mu_l = d_l / |d_l|, kappa_l = exp(clip(r_l, -3, 5)) + 1e-3
   loss    mean over samples of -c_i log q(w_i)
 With bf16=True the GPU's roundings are applied: weights, the encoded input
-and hidden activations to BF16; the head gradient to BF16 where it feeds the
-tensor-core product dY W.
+and hidden activations to BF16; every layer's output gradient dY to BF16,
+as it enters the tensor-core products dY W, dY^T X and the bias sums.
 """
 from __future__ import annotations
 
@@ -143,10 +143,10 @@ def gradient(p, feat, dirs, c, use_bf16=False) -> np.ndarray:
     for l in range(4, -1, -1):
         W, _ = layers[l]
         x = xs[l]
-        grads[l] = (dy.T @ x, dy.sum(axis=0))
+        dyq = bf16(dy) if use_bf16 else dy
+        grads[l] = (dyq.T @ x, dyq.sum(axis=0))
         if l == 0:
             break
-        dyq = bf16(dy) if use_bf16 else dy
         Wq = bf16(W) if use_bf16 else W
         dx = dyq @ Wq
         dy = dx * (x > 0)

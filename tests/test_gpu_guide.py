@@ -85,3 +85,34 @@ def test_training_fits_a_direction_field(ctx):
     raw = g.forward(feat)
     q = mo.mixture_pdf(raw.astype(np.float64), d.astype(np.float64))
     assert np.median(q) > 5 / (4 * np.pi)   # far above the uniform density
+
+
+def test_adam_step_fused_into_backward(ctx):
+    """One training step: the backward's last CTA applies Adam (first step:
+    p -= lr * g / (|g| + eps), i.e. lr times the sign of the mean gradient),
+    repacks the BF16 operands (the next forward uses the new weights) and
+    leaves a zero gradient for the next step, also after a gradient query."""
+    p = mo.init_params(13).astype(np.float32)
+    feat, d, c = batch(3000, 14)
+    ref = mo.gradient(p.astype(np.float64), feat.astype(np.float64), d.astype(np.float64), c.astype(np.float64),
+                      use_bf16=True) / feat.shape[0]
+    lr = 1e-3
+    a = tg.Guide(ctx, seed=3)
+    a.set_params(p)
+    a.gradient(feat, d, c)            # leaves its gradient in the device buffer
+    a.train(feat, d, c, lr=lr, steps=1)
+    pa = a.get_params()
+    step = (p - pa) / lr
+    big = np.abs(ref) > 1e-5
+    assert np.abs(step).max() <= 1.0 + 1e-3
+    assert (np.sign(step[big]) == np.sign(ref[big])).mean() > 0.99
+    assert (np.abs(step[big]) > 0.9).mean() > 0.99
+    # the same step on a guide that never answered a gradient query
+    b = tg.Guide(ctx, seed=3)
+    b.set_params(p)
+    b.train(feat, d, c, lr=lr, steps=1)
+    assert np.allclose(b.get_params(), pa, atol=1e-5)
+    # the repacked BF16 operands: the forward now computes with the new weights
+    out = a.forward(feat[:500])
+    want, _ = mo.forward(pa.astype(np.float64), feat[:500].astype(np.float64), use_bf16=True)
+    assert rel(out, want) < 1e-2

@@ -125,6 +125,31 @@ def test_launch_shape_is_invisible(ctx):
     assert np.array_equal(a, b) and sa.rays == sb.rays
 
 
+def test_refill_thresholds_are_invisible(ctx):
+    """The warp refill threshold of every ray kind (1 or 32 idle lanes)
+    changes scheduling only: same image bits, same ray counts, same hits."""
+    m, sid, ref = setup(ctx, kind=tg.SCENE_SPHERE_ROOM, detail=4)
+    job = tg.make_job(sid, m, 64, 40, pixel_samples=4, max_depth=3, seed=13)
+    (a,), (sa,) = ctx.render([job])
+    o, d = tg.make_rays(50_000, ref.box, seed=5)
+    hits = ctx.intersect(sid, o, d)
+    kinds = (tg.RAYS_PRIMARY, tg.RAYS_BOUNCE, tg.RAYS_SHADOW_PRIMARY, tg.RAYS_SHADOW, tg.RAYS_INTERSECT)
+    defaults = (32, 2, 32, 4, 1)
+    try:
+        for lanes in (1, 7, 32):
+            for k in kinds:
+                ctx.set_traversal_refill(k, lanes)
+            (b,), (sb,) = ctx.render([job])
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and sa.rays == sb.rays
+            h2 = ctx.intersect(sid, o, d)
+            assert all(np.array_equal(x.view(np.uint32), y.view(np.uint32)) for x, y in zip(hits, h2))
+        with pytest.raises(tg.TurnerError):
+            ctx.set_traversal_refill(tg.RAYS_BOUNCE, 33)
+    finally:
+        for k, v in zip(kinds, defaults):
+            ctx.set_traversal_refill(k, v)
+
+
 def test_render_is_deterministic(ctx):
     m, sid, _ = setup(ctx, kind=tg.SCENE_ROOM)
     job = tg.make_job(sid, m, 32, 32, pixel_samples=4, max_depth=3, seed=8)

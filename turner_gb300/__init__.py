@@ -51,6 +51,7 @@ SCENE_MIRROR_ROOM = 5
 TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
 GRAPH_AUTO, GRAPH_ALWAYS, GRAPH_NEVER = 0, 1, 2
+RAYS_PRIMARY, RAYS_BOUNCE, RAYS_SHADOW_PRIMARY, RAYS_SHADOW, RAYS_INTERSECT = 0, 1, 2, 3, 4
 RENDERER_PATH, RENDERER_RAYTRACE, RENDERER_RAYCAST = 0, 1, 2
 KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect", "k_guide_features",
                 "k_mlp_forward", "guide_train")
@@ -129,6 +130,7 @@ def _lib() -> C.CDLL:
         "turner_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
         "turner_graph_launch_count": (C.c_uint64, [_P]),
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
+        "turner_set_traversal_refill": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
@@ -420,6 +422,11 @@ class Context:
         _check(_lib().turner_probe_gather(self._h, buffer_bytes, load_bytes, repeats, C.byref(v)),
                "turner_probe_gather")
         return v.value
+
+    def set_traversal_refill(self, kind: int, lanes: int) -> None:
+        """A warp of the persistent traversal takes new rays of this kind
+        (RAYS_*) only once `lanes` of its lanes are idle."""
+        _check(_lib().turner_set_traversal_refill(self._h, kind, lanes), "turner_set_traversal_refill")
 
     def set_profiling(self, on: bool) -> None:
         _check(_lib().turner_set_profiling(self._h, 1 if on else 0), "turner_set_profiling")

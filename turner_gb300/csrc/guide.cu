@@ -10,11 +10,12 @@
 // write the next layer's operand with 16-byte stores.
 //
 // Backward (k_mlp_backward): per tile, the vMF-mixture head gradient of the
-// loss -c log q(w) (one thread per sample), then per layer from the top:
-// dW += dY^T X and db += sum dY on the CUDA cores from shared memory (FP32),
-// and dX = dY W on the tensor cores (a second BF16 copy of the weights,
-// transposed), masked by ReLU'. Each CTA accumulates its gradient in shared
-// memory and adds it to the global one once.
+// loss -c log q(w) (one thread per sample), then per layer from the top, on
+// the tensor cores: dX = dY W (a second BF16 copy of the weights,
+// transposed), masked by ReLU', and [dW, db] += dY^T [X, 1] accumulated in
+// TMEM over all of a CTA's tiles. Each CTA adds its gradient to the global one
+// once; in a training step the last CTA applies Adam and repacks the BF16
+// weights.
 //
 // Every mbarrier wait is bounded; a timeout sets *err and the kernel drains
 // its outstanding MMA (bounded), frees its TMEM and returns.
@@ -34,7 +35,6 @@
 namespace turner {
 namespace guide {
 
-constexpr int kThreads = 128;
 constexpr uint32_t kTmemCols = 64;
 
 struct Weights {
@@ -240,16 +240,62 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
 }
 
 // ---------------------------------------------------------------- backward
+// One CTA of 256 threads per SM, tiles of 128 samples. Per tile, the head
+// gradient dY_5 of -c log q (threads 0-127, one sample each), then per layer
+// from the top, with X_l and dY_l staged row-major in shared memory:
+//   dX   = dY W          M = 128 samples, N = 64 inputs, K = outputs (48 / 64)
+//   dW' += dY^T [X, 1]   M = 128 (output units in rows 0-63, rows 64-127 zero),
+//                        N = inputs + a ones column (the bias gradient) padded
+//                        to 80 / 96, K = 128 samples
+// both on tcgen05 with BF16 operands in the core-matrix K-major layout. The
+// transposed operands dY^T and [X, 1]^T are built in shared memory from the
+// row-major staging buffers. dW' stays in TMEM for all of the CTA's tiles
+// (480 of the 512 columns: dX 64, then 96 + 4 x 80); at the end each CTA adds
+// it to the global gradient once, and with `adam` set the last CTA to finish
+// applies the Adam step, repacks the BF16 operand tiles and clears the
+// gradient for the next step (no separate Adam or pack launches).
+constexpr int kBwdThreads = 256;
+constexpr uint32_t kBwdTmemCols = 512;
+constexpr int kXRow = 88, kDyRow = 72;   // row strides (elements) of the staging buffers
+__host__ __device__ constexpr int dw_n(int l) { return l == 0 ? 96 : 80; }
+__host__ __device__ constexpr int dw_col(int l) { return l == 0 ? 64 : 160 + 80 * (l - 1); }
+static_assert(dw_col(4) + dw_n(4) <= static_cast<int>(kBwdTmemCols), "TMEM columns");
+
 struct BwdSmem {
-    uint8_t wt[kBwdBytes];             // W_l^T operands, layers 1..4 (0-based)
-    uint8_t dy_km[kHidden * 128 * 2];  // dY, BF16, K-major 128 x 64 (or 48)
-    float dy[128][kHidden + 1];        // dY, FP32, row per sample (+1 avoids bank conflicts)
-    __nv_bfloat16 x[128][kIn + 2];     // X_l, row per sample
-    float grad[kParams];               // this CTA's gradient
+    uint8_t wt[kBwdBytes];                 // W_l^T operands, layers 1..4 (B of dX)
+    uint8_t dy_km[128 * kHidden * 2];      // dY, K-major 128 x 48 / 64 (A of dX)
+    uint8_t dyT[128 * 128 * 2];            // dY^T, K-major 128 x 128 samples, rows 64.. zero (A of dW)
+    uint8_t xT[96 * 128 * 2];              // [X, 1]^T, K-major 80 / 96 x 128 samples (B of dW)
+    __nv_bfloat16 xrow[128 * kXRow];       // X_l, row per sample
+    __nv_bfloat16 dyrow[128 * kDyRow];     // dY_l, row per sample
     uint64_t mbar;
     uint32_t tmem;
     int abort;
+    int last;
     float loss;
+};
+
+// Per-step training state, resident on the device so that a training step
+// needs no host synchronisation: the sample count may come from a device
+// counter (the records of a render pass).
+struct TrainState {
+    uint32_t n;        // samples of this step
+    int32_t skip;      // fewer than the step's minimum: no update
+    uint32_t step;     // Adam steps taken
+    float bc1, bc2;    // bias corrections of this step
+    float scale;       // 1 / n (the loss is a mean over samples)
+    float loss_mean;   // loss of the last step / n
+    uint32_t done;     // backward CTAs finished in this step (the last one updates)
+};
+
+struct AdamArgs {
+    float* params;     // FP32 master
+    float* m;
+    float* v;
+    uint8_t* fwd;      // packed BF16 operands, rewritten after the update
+    uint8_t* bwd;
+    TrainState* state;
+    float lr, b1, b2, eps;
 };
 
 // Head gradient of L = -c log q(w): writes dL/d raw (40) and returns L.
@@ -290,50 +336,123 @@ __device__ __forceinline__ float head_grad(const float raw[kOut], const float di
     return loss;
 }
 
+__device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 h) { return static_cast<uint32_t>(__bfloat16_as_ushort(h)); }
+
+// Eight BF16 values p[0], p[stride], ..., p[7 stride] as one 16-byte chunk.
+__device__ __forceinline__ uint4 gather8(const __nv_bfloat16* p, int stride) {
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = bf16_bits(p[(2 * i) * stride]) | (bf16_bits(p[(2 * i + 1) * stride]) << 16);
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// X_l of the tile's 128 samples from the forward's activations (336 BF16 per
+// sample: X_0 80, X_1..X_4 64 each), row-major into xrow; zeros past n.
+__device__ __forceinline__ void stage_x(BwdSmem& sm, const __nv_bfloat16* __restrict__ acts, uint32_t n, uint32_t s0,
+                                        int l, int t, int nt) {
+    const int chunks = layer_in(l) / 8;
+    const int off = l == 0 ? 0 : 80 + 64 * (l - 1);
+    for (int i = t; i < 128 * chunks; i += nt) {
+        const int r = i / chunks, c = i - r * chunks;
+        const uint32_t s = s0 + static_cast<uint32_t>(r);
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (s < n) v = *reinterpret_cast<const uint4*>(acts + size_t(s) * 336 + off + 8 * c);
+        *reinterpret_cast<uint4*>(sm.xrow + r * kXRow + 8 * c) = v;
+    }
+}
+
+// [X_l, 1]^T (rows: the layer's inputs, then a ones row, then zero rows up to
+// dw_n(l)) and dY^T (rows: output units below n_pad, zeros up to 64), both
+// K-major over the 128 samples, from the staging buffers.
+__device__ __forceinline__ void build_transposes(BwdSmem& sm, int l) {
+    const int K = layer_in(l), N = dw_n(l), npad = layer_out_pad(l);
+    const uint32_t one2 = 0x3F803F80u;   // two BF16 ones
+    for (int c = threadIdx.x; c < N * 16; c += kBwdThreads) {
+        const int k = c % N, j = c / N;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (k < K) u = gather8(sm.xrow + (8 * j) * kXRow + k, kXRow);
+        else if (k == K) u = make_uint4(one2, one2, one2, one2);
+        *reinterpret_cast<uint4*>(sm.xT + tc::kmajor_offset(static_cast<uint32_t>(k), 8u * j, 128)) = u;
+    }
+    for (int c = threadIdx.x; c < kHidden * 16; c += kBwdThreads) {
+        const int o = c % kHidden, j = c / kHidden;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (o < npad) u = gather8(sm.dyrow + (8 * j) * kDyRow + o, kDyRow);
+        *reinterpret_cast<uint4*>(sm.dyT + tc::kmajor_offset(static_cast<uint32_t>(o), 8u * j, 128)) = u;
+    }
+}
+
+// D (+)= A * B^T over K / 16 steps of K-major operands with R-row groups of
+// K / 8 core matrices (no commit).
+__device__ __forceinline__ void issue_steps(uint32_t tmem, const uint8_t* a, const uint8_t* b, int K, int N,
+                                            bool accumulate) {
+    const uint32_t sa = tc::smem_u32(a), sb = tc::smem_u32(b);
+    const uint32_t sbo = static_cast<uint32_t>(K / 8) * 128u;
+    const uint32_t idesc = tc::idesc_bf16(128, static_cast<uint32_t>(N));
+    for (int i = 0; i < K / 16; ++i) {
+        const uint64_t ad = tc::smem_desc(sa + 256u * i, 128u, sbo);
+        const uint64_t bd = tc::smem_desc(sb + 256u * i, 128u, sbo);
+        tc::mma_bf16(tmem, ad, bd, idesc, accumulate || i > 0);
+    }
+}
+
 // features/acts/out as produced by k_mlp_forward for the same samples;
-// dirs: n x 3 unit directions; weight: n target weights c. grad += dLoss/dparams.
-__global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const uint32_t* __restrict__ n_dev,
-                                                              const __nv_bfloat16* __restrict__ acts,
-                                                              const float* __restrict__ out,
-                                                              const float* __restrict__ dirs,
-                                                              const float* __restrict__ weight, Weights wts,
-                                                              float* __restrict__ grad, float* __restrict__ loss_sum,
-                                                              int* err) {
+// dirs: n x 3 unit directions; weight: n target weights c. grad += dLoss/dparams;
+// with do_adam, the last CTA then takes the Adam step (see above).
+__global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
+    uint32_t n, const uint32_t* __restrict__ n_dev, const __nv_bfloat16* __restrict__ acts,
+    const float* __restrict__ out, const float* __restrict__ dirs, const float* __restrict__ weight, Weights wts,
+    float* __restrict__ grad, float* __restrict__ loss_sum, int* err, AdamArgs adam, int do_adam) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (n_dev) n = min(n, *n_dev);
-    for (int i = tid; i < kBwdBytes / 16; i += kThreads) {
+    for (int i = tid; i < kBwdBytes / 16; i += kBwdThreads) {
         reinterpret_cast<uint4*>(sm.wt)[i] = reinterpret_cast<const uint4*>(wts.bwd)[i];
     }
-    for (int i = tid; i < kParams; i += kThreads) sm.grad[i] = 0.f;
+    // rows 64..127 of dY^T are never written again: zero the whole buffer once
+    for (int i = tid; i < static_cast<int>(sizeof(sm.dyT) / 16); i += kBwdThreads) {
+        reinterpret_cast<uint4*>(sm.dyT)[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
     if (tid == 0) {
         sm.abort = 0;
+        sm.last = 0;
         sm.loss = 0.f;
         tc::mbar_init(&sm.mbar, 1);
         tc::fence_mbar_init();
     }
-    if (warp == 0) tc::tmem_alloc(&sm.tmem, kTmemCols);
+    if (warp == 0) tc::tmem_alloc(&sm.tmem, kBwdTmemCols);
     tc::fence_async_smem();
     tc::tc_fence_before_sync();
     __syncthreads();
     tc::tc_fence_after_sync();
     const uint32_t tmem = sm.tmem;
-    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const uint32_t quad = static_cast<uint32_t>(warp & 3), colh = static_cast<uint32_t>(warp >> 2);
+    const uint32_t lane_base = (quad * 32u) << 16;
     uint32_t phase = 0;
     const uint32_t tiles = (n + 127) / 128;
     float my_loss = 0.f;
+    bool had_tile = false;
 
     for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
-        const uint32_t s = tile * 128 + tid;
-        const bool valid = s < n;
-        // head: dY of the output layer, 40 columns padded to 48
-        {
+        const bool first = !had_tile;
+        had_tile = true;
+        const uint32_t s0 = tile * 128;
+        if (tid < 128) {
+            // head: dY of the output layer, 40 columns padded to 48
+            const uint32_t s = s0 + static_cast<uint32_t>(tid);
             float g[kOut];
-            if (valid) {
+            if (s < n) {
                 float raw[kOut];
+                const float4* o4 = reinterpret_cast<const float4*>(out + size_t(s) * kOut);
 #pragma unroll
-                for (int k = 0; k < kOut; ++k) raw[k] = out[size_t(s) * kOut + k];
+                for (int q = 0; q < kOut / 4; ++q) {
+                    const float4 v = o4[q];
+                    raw[4 * q] = v.x;
+                    raw[4 * q + 1] = v.y;
+                    raw[4 * q + 2] = v.z;
+                    raw[4 * q + 3] = v.w;
+                }
                 const float d[3] = {dirs[3 * size_t(s)], dirs[3 * size_t(s) + 1], dirs[3 * size_t(s) + 2]};
                 my_loss += head_grad(raw, d, weight[s], g);
             } else {
@@ -341,115 +460,154 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_backward(uint32_t n, const 
                 for (int k = 0; k < kOut; ++k) g[k] = 0.f;
             }
 #pragma unroll
-            for (int k = 0; k < kOutPad; ++k) {
-                const float v = k < kOut ? g[k] : 0.f;
-                sm.dy[tid][k] = v;
-                store_bf16(sm.dy_km, tc::kmajor_offset(tid, k, kOutPad), v);
+            for (int q = 0; q < kOutPad / 8; ++q) {
+                float y[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) y[j] = 8 * q + j < kOut ? g[8 * q + j] : 0.f;
+                const uint4 u = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]), pack_bf16x2(y[4], y[5]),
+                                           pack_bf16x2(y[6], y[7]));
+                *reinterpret_cast<uint4*>(sm.dyrow + tid * kDyRow + 8 * q) = u;
+                *reinterpret_cast<uint4*>(sm.dy_km + tc::kmajor_offset(static_cast<uint32_t>(tid), 8u * q, kOutPad)) = u;
             }
+        } else {
+            stage_x(sm, acts, n, s0, kLayers - 1, tid - 128, 128);
         }
         for (int l = kLayers - 1; l >= 0; --l) {
-            const int K_in = layer_in(l), n_out = layer_out(l), n_pad = layer_out_pad(l);
-            // X_l rows of this tile
-            for (int k = 0; k < K_in; ++k) {
-                sm.x[tid][k] = valid ? acts[size_t(s) * 336 + (l == 0 ? 0 : 80 + 64 * (l - 1)) + k]
-                                     : __float2bfloat16_rn(0.f);
-            }
+            // xrow = X_l, dyrow / dy_km = dY_l
+            __syncthreads();
+            build_transposes(sm, l);
             tc::fence_async_smem();
             tc::tc_fence_before_sync();
             __syncthreads();
             tc::tc_fence_after_sync();
-            // dX = dY W on the tensor cores (not needed below the first layer)
-            if (l > 0 && tid == 0) issue_layer(tmem, sm.dy_km, sm.wt + bwd_off(l), n_pad, K_in, &sm.mbar);
-            // dW_l += dY^T X_l, db_l += sum dY on the CUDA cores meanwhile
-            const int wbase = layer_w(l), bbase = layer_b(l);
-            for (int e = tid; e < n_out * K_in; e += kThreads) {
-                const int o = e / K_in, k = e - o * K_in;
-                float acc = 0.f;
-                for (int r = 0; r < 128; ++r) acc += sm.dy[r][o] * __bfloat162float(sm.x[r][k]);
-                sm.grad[wbase + e] += acc;
+            if (tid == 0) {
+                // dX = dY W (not needed below the first layer), then dW' += dY^T [X, 1]
+                if (l > 0) issue_steps(tmem, sm.dy_km, sm.wt + bwd_off(l), layer_out_pad(l), layer_in(l), false);
+                issue_steps(tmem + static_cast<uint32_t>(dw_col(l)), sm.dyT, sm.xT, 128, dw_n(l), !first);
+                tc::mma_commit(&sm.mbar);
             }
-            if (tid < n_out) {
-                float acc = 0.f;
-                for (int r = 0; r < 128; ++r) acc += sm.dy[r][tid];
-                sm.grad[bbase + tid] += acc;
-            }
-            if (l > 0) {
-                if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
-                phase ^= 1;
-                tc::tc_fence_after_sync();
-            }
-            __syncthreads();   // dY and X_l are no longer read
+            if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
+            phase ^= 1;
+            tc::tc_fence_after_sync();
+            __syncthreads();
             if (sm.abort || l == 0) break;
-            // dY of the layer below: dX masked by ReLU' (X_l > 0)
-            for (int c0 = 0; c0 < K_in; c0 += 16) {
-                float v[16];
-                tc::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), v);
+            // dY of the layer below: dX masked by ReLU' (X_l > 0); warp w reads
+            // lanes 32 (w % 4).. (its samples) and columns 32 (w / 4)..
+            {
+                const int r = static_cast<int>(quad) * 32 + lane;
+                const uint32_t c0 = colh * 32u;
+                float v[32];
+                tc::tmem_ld16(tmem + lane_base + c0, v);
+                tc::tmem_ld16(tmem + lane_base + c0 + 16u, v + 16);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int c = c0 + j;
-                    const float d = __bfloat162float(sm.x[tid][c]) > 0.f ? v[j] : 0.f;
-                    sm.dy[tid][c] = d;
-                    store_bf16(sm.dy_km, tc::kmajor_offset(tid, c, kHidden), d);
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 xv = *reinterpret_cast<const uint4*>(sm.xrow + r * kXRow + c0 + 8 * q);
+                    const uint32_t xw[4] = {xv.x, xv.y, xv.z, xv.w};
+                    float y[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const uint32_t h = (xw[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;   // BF16 bits of X
+                        y[j] = __uint_as_float(h << 16) > 0.f ? v[8 * q + j] : 0.f;
+                    }
+                    const uint4 u = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]),
+                                               pack_bf16x2(y[4], y[5]), pack_bf16x2(y[6], y[7]));
+                    *reinterpret_cast<uint4*>(sm.dyrow + r * kDyRow + c0 + 8 * q) = u;
+                    *reinterpret_cast<uint4*>(sm.dy_km + tc::kmajor_offset(static_cast<uint32_t>(r), c0 + 8u * q,
+                                                                           kHidden)) = u;
                 }
             }
-            tc::fence_async_smem();
-            tc::tc_fence_before_sync();
-            __syncthreads();
-            tc::tc_fence_after_sync();
+            __syncthreads();   // X_l is no longer read
+            stage_x(sm, acts, n, s0, l - 1, tid, kBwdThreads);
         }
     }
-    // loss and gradient out
+    // loss, and this CTA's dW' out of TMEM into the global gradient
     for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_xor_sync(0xFFFFFFFFu, my_loss, off);
-    if ((tid & 31) == 0) atomicAdd(&sm.loss, my_loss);
+    if (lane == 0) atomicAdd(&sm.loss, my_loss);
     if (sm.abort && tid == 0) tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
     tc::tc_fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
-    for (int i = tid; i < kParams; i += kThreads) {
-        if (sm.grad[i] != 0.f) atomicAdd(grad + i, sm.grad[i]);
+    tc::tc_fence_after_sync();
+    if (had_tile && !sm.abort && quad < 2) {
+        const int o = static_cast<int>(quad) * 32 + lane;   // output unit = TMEM lane
+#pragma unroll 1
+        for (int l = 0; l < kLayers; ++l) {
+            const int K = layer_in(l), N = dw_n(l), nout = layer_out(l);
+            for (int c = static_cast<int>(colh) * 16; c < N; c += 32) {
+                float v[16];
+                tc::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(dw_col(l) + c), v);
+                if (o < nout) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int k = c + j;
+                        if (k < K) atomicAdd(grad + layer_w(l) + o * K + k, v[j]);
+                        else if (k == K) atomicAdd(grad + layer_b(l) + o, v[j]);
+                    }
+                }
+            }
+        }
     }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kBwdTmemCols);
     if (tid == 0 && loss_sum) atomicAdd(loss_sum, sm.loss);
+    if (!do_adam) return;
+    // the last CTA to finish takes the Adam step on the complete gradient
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) sm.last = atomicAdd(&adam.state->done, 1u) == gridDim.x - 1 ? 1 : 0;
+    __syncthreads();
+    if (!sm.last) return;
+    __threadfence();
+    TrainState* st = adam.state;
+    if (!st->skip) {
+        const float scale = st->scale, bc1 = st->bc1, bc2 = st->bc2;
+        for (int i = tid; i < kParams; i += kBwdThreads) {
+            const float gi = __ldcg(grad + i) * scale;
+            const float mi = adam.b1 * adam.m[i] + (1.f - adam.b1) * gi;
+            const float vi = adam.b2 * adam.v[i] + (1.f - adam.b2) * gi * gi;
+            adam.m[i] = mi;
+            adam.v[i] = vi;
+            adam.params[i] -= adam.lr * (mi / bc1) / (sqrtf(vi / bc2) + adam.eps);
+        }
+        if (tid == 0 && loss_sum) st->loss_mean = __ldcg(loss_sum) * scale;
+        __syncthreads();
+        // BF16 operand tiles from the updated parameters
+        for (int l = 0; l < kLayers; ++l) {
+            const int K = layer_in(l), nout = layer_out(l), pad = layer_out_pad(l);
+            const float* W = adam.params + layer_w(l);
+            for (int e = tid; e < pad * K; e += kBwdThreads) {
+                const int r = e / K, k = e - r * K;
+                const float w = r < nout ? W[r * K + k] : 0.f;
+                store_bf16(adam.fwd + fwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(r), static_cast<uint32_t>(k),
+                                                                    static_cast<uint32_t>(K)), w);
+                if (l > 0) {
+                    store_bf16(adam.bwd + bwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(k),
+                                                                        static_cast<uint32_t>(r),
+                                                                        static_cast<uint32_t>(pad)), w);
+                }
+            }
+        }
+    }
+    // a clean gradient for the next step
+    for (int i = tid; i < kParams; i += kBwdThreads) grad[i] = 0.f;
+    if (tid == 0) {
+        if (loss_sum) *loss_sum = 0.f;
+        st->done = 0;
+    }
 }
 
 // ------------------------------------------------------------ Adam + pack
-// Per-step training state, resident on the device so that a training step
-// needs no host synchronisation: the sample count may come from a device
-// counter (the records of a render pass).
-struct TrainState {
-    uint32_t n;        // samples of this step
-    int32_t skip;      // fewer than the step's minimum: no update
-    uint32_t step;     // Adam steps taken
-    float bc1, bc2;    // bias corrections of this step
-    float scale;       // 1 / n (the loss is a mean over samples)
-    float loss_mean;   // loss of the last step / n
-};
-
 __global__ void k_train_prep(const uint32_t* __restrict__ n_dev, uint32_t n, uint32_t min_n, TrainState* s, float b1,
                              float b2) {
     if (n_dev) n = min(n, *n_dev);
     s->n = n;
     s->skip = n < min_n ? 1 : 0;
+    s->done = 0;
     if (s->skip) return;
     s->step += 1;
     s->bc1 = 1.f - powf(b1, static_cast<float>(s->step));
     s->bc2 = 1.f - powf(b2, static_cast<float>(s->step));
     s->scale = 1.f / static_cast<float>(n);
-}
-
-__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
-                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps, TrainState* s,
-                       const float* __restrict__ loss_sum) {
-    if (s->skip) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) s->loss_mean = *loss_sum * s->scale;
-    if (i >= n) return;
-    const float scale = s->scale, bc1 = s->bc1, bc2 = s->bc2;
-    const float gi = g[i] * scale;
-    const float mi = b1 * m[i] + (1.f - b1) * gi;
-    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
 }
 
 // BF16 operand tiles from the FP32 parameters.
@@ -497,6 +655,7 @@ struct turner_guide {
     float* wts = nullptr;
     float* out = nullptr;
     __nv_bfloat16* acts = nullptr;
+    bool grad_dirty = false;   // grad / loss hold a turner_guide_gradient result, not zeros
     int sms = 1;
     double train_ms = 0, infer_ms = 0;
     uint64_t train_steps = 0;
@@ -611,17 +770,19 @@ int train_device(turner_guide* g, const float* feat, const float* dirs, const fl
     if (st != TURNER_OK) return st;
     Weights w{g->fwd, g->bwd, g->params};
     const float b1 = 0.9f, b2 = 0.999f;
-    GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), stream));
-    GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), stream));
+    if (g->grad_dirty) {
+        // the backward's last CTA leaves them zero; only a gradient query does not
+        GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), stream));
+        GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), stream));
+        g->grad_dirty = false;
+    }
     k_train_prep<<<1, 1, 0, stream>>>(n_dev, n, min_n, g->state, b1, b2);
     const uint32_t* n_step = &g->state->n;
     k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), stream>>>(n, n_step, feat, w, g->out, g->acts,
                                                                              g->err);
-    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), stream>>>(n, n_step, g->acts, g->out, dirs, wts, w,
-                                                                      g->grad, g->loss, g->err);
-    k_adam<<<(kParams + 255) / 256, 256, 0, stream>>>(g->params, g->grad, g->m, g->v, kParams, lr, b1, b2, 1e-8f,
-                                                      g->state, g->loss);
-    k_pack<<<dim3(16, kLayers), 256, 0, stream>>>(g->params, g->fwd, g->bwd);
+    const AdamArgs adam{g->params, g->m, g->v, g->fwd, g->bwd, g->state, lr, b1, b2, 1e-8f};
+    k_mlp_backward<<<grid_tiles(g, n), kBwdThreads, bwd_smem(), stream>>>(n, n_step, g->acts, g->out, dirs, wts, w,
+                                                                         g->grad, g->loss, g->err, adam, 1);
     GCK(cudaGetLastError());
     g->train_steps += 1;
     if (loss_out) {
@@ -707,6 +868,8 @@ int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
     if (e == cudaSuccess) e = cudaMemset(g->v, 0, kParams * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(g->state, 0, sizeof(TrainState));
+    if (e == cudaSuccess) e = cudaMemset(g->grad, 0, kParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(g->loss, 0, sizeof(float));
     if (e == cudaSuccess) {
         k_pack<<<dim3(16, kLayers), 256, 0, g->stream>>>(g->params, g->fwd, g->bwd);
         e = cudaStreamSynchronize(g->stream);
@@ -772,10 +935,12 @@ int turner_guide_gradient(turner_guide* g, const float* features, const float* d
     GCK(cudaMemcpyAsync(g->wts, weights, n * sizeof(float), cudaMemcpyHostToDevice, g->stream));
     GCK(cudaMemsetAsync(g->grad, 0, kParams * sizeof(float), g->stream));
     GCK(cudaMemsetAsync(g->loss, 0, sizeof(float), g->stream));
+    g->grad_dirty = true;
     Weights w{g->fwd, g->bwd, g->params};
     k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), g->stream>>>(n, nullptr, g->feat, w, g->out, g->acts, g->err);
-    k_mlp_backward<<<grid_tiles(g, n), kThreads, bwd_smem(), g->stream>>>(n, nullptr, g->acts, g->out, g->dirs,
-                                                                         g->wts, w, g->grad, g->loss, g->err);
+    k_mlp_backward<<<grid_tiles(g, n), kBwdThreads, bwd_smem(), g->stream>>>(n, nullptr, g->acts, g->out, g->dirs,
+                                                                            g->wts, w, g->grad, g->loss, g->err,
+                                                                            AdamArgs{}, 0);
     GCK(cudaGetLastError());
     GCK(cudaMemcpyAsync(grad_out, g->grad, kParams * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     float l = 0;

@@ -102,6 +102,7 @@ struct TraverseCfg {
     bool mailbox = false;         // skip repeated tests of a triangle (128-thread blocks)
     unsigned min_blocks = 10;     // 10, 12, 16: cap registers so that many blocks fit per SM (128-thread
                                   // blocks); 0: no cap. 10 (48 registers) is fastest on GB300
+    unsigned refill = 1;          // persistent: a warp takes new rays once this many lanes are idle (1..32)
     uint32_t* work = nullptr;
 };
 

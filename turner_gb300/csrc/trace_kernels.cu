@@ -664,40 +664,48 @@ struct OccSrc {             // turner_occluded batches: any hit with r <= tmax[i
 };
 
 // Persistent traversal: each lane holds one ray; lanes whose ray is finished
-// take the next unclaimed ray (one atomicAdd per warp), so warps stay full
-// while rays of very different lengths are traversed. MULTI: every ray names
-// its job and is traced in that job's scene.
+// take the next unclaimed rays (one atomicAdd per warp), so warps stay full
+// while rays of very different lengths are traversed. A warp refills only
+// once at least `refill` of its lanes are idle (or none is active): 1 refills
+// every round and keeps the most lanes busy; 32 refills whole warps, so
+// neighbouring rays of a coherent queue (camera rays) stay together and share
+// node and record loads. MULTI: every ray names its job and is traced in
+// that job's scene.
 template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, class Stack>
 __device__ __forceinline__ void traverse_persistent(const SceneView& single, const JobDesc* __restrict__ jobs,
-                                                    Src& src, uint32_t* __restrict__ work, Stack& st) {
+                                                    Src& src, uint32_t* __restrict__ work, uint32_t refill,
+                                                    Stack& st) {
     const uint32_t n = src.count();
     TravState s;
     uint32_t cur = 0;
     bool active = false, exhausted = false;
     float tmax = 0.f;
     for (;;) {
-        for (;;) {
-            const bool need = !active && !exhausted;
-            const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
-            if (mask == 0) break;
-            const int leader = __ffs(mask) - 1;
-            uint32_t base = 0;
-            if (static_cast<int>(lane_id()) == leader) base = atomicAdd(work, static_cast<uint32_t>(__popc(mask)));
-            base = __shfl_sync(0xFFFFFFFFu, base, leader);
-            if (need) {
-                const uint32_t idx = base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
-                if (idx >= n) {
-                    exhausted = true;
-                } else {
-                    float3 o, d;
-                    uint32_t job;
-                    src.load(idx, o, d, tmax, job);
-                    const bool in_box = MULTI ? trav_begin(jobs[job].sc, o, d, s) : trav_begin(single, o, d, s);
-                    if (in_box) {
-                        cur = idx;
-                        active = true;
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
+        if (idle && (static_cast<uint32_t>(__popc(idle)) >= refill || __ballot_sync(0xFFFFFFFFu, active) == 0)) {
+            for (;;) {
+                const bool need = !active && !exhausted;
+                const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
+                if (mask == 0) break;
+                const int leader = __ffs(mask) - 1;
+                uint32_t base = 0;
+                if (static_cast<int>(lane_id()) == leader) base = atomicAdd(work, static_cast<uint32_t>(__popc(mask)));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (need) {
+                    const uint32_t idx = base + static_cast<uint32_t>(__popc(mask & ((1u << lane_id()) - 1u)));
+                    if (idx >= n) {
+                        exhausted = true;
                     } else {
-                        src.store(idx, s.best);   // misses the scene box
+                        float3 o, d;
+                        uint32_t job;
+                        src.load(idx, o, d, tmax, job);
+                        const bool in_box = MULTI ? trav_begin(jobs[job].sc, o, d, s) : trav_begin(single, o, d, s);
+                        if (in_box) {
+                            cur = idx;
+                            active = true;
+                        } else {
+                            src.store(idx, s.best);   // misses the scene box
+                        }
                     }
                 }
             }
@@ -716,16 +724,17 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
 // the uncapped kernel gives only the block size.
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX>
 __global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
-                                                     uint32_t* __restrict__ work) {
+                                                     uint32_t* __restrict__ work, uint32_t refill) {
     LocalStack<STACK> st;
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, st);
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
 }
 
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_traverse_capped(SceneView single, const JobDesc* __restrict__ jobs,
-                                                                  Src src, uint32_t* __restrict__ work) {
+                                                                  Src src, uint32_t* __restrict__ work,
+                                                                  uint32_t refill) {
     LocalStack<STACK> st;
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, st);
+    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
 }
 
 // Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
@@ -807,12 +816,12 @@ template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
 void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
                         const TraverseCfg& cfg, cudaStream_t stream) {
-    void (*kernel)(SceneView, const JobDesc*, Src, uint32_t*);
+    void (*kernel)(SceneView, const JobDesc*, Src, uint32_t*, uint32_t);
     if constexpr (MINB > 1) kernel = k_traverse_capped<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB>;
     else kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX>;
     const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
     const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm), std::max(1u, need));
-    kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work);
+    kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work, std::max(1u, std::min(32u, cfg.refill)));
 }
 
 // Dispatch on the tuned block size and stack depth. The stack must hold the
