@@ -259,12 +259,13 @@ def run_batch64(args) -> None:
     depths = rng.integers(1, 6, n)
     ctx = tg.Context(0)
     t0 = time.perf_counter()
-    jobs, tris = [], 0
+    jobs, tris, scenes = [], 0, []
     for k in range(n):
         m = tg.make_scene(tg.SCENE_SOUP, count=int(counts[k]), seed=1000 + k)
         tree = tg.KDTree.build_gpu(ctx, m) if args.gpu_build else tg.KDTree.from_mesh(m)
         sid = ctx.upload_tree(tree)
         tris += m.n_triangles
+        scenes.append((m, tree))
         jobs.append(tg.make_job(sid, m, int(sides[k]), int(sides[k]), pixel_samples=int(spps[k]),
                                 max_depth=int(depths[k]), seed=77 + k))
     build_s = time.perf_counter() - t0
@@ -294,9 +295,35 @@ def run_batch64(args) -> None:
                    "graph_launches_per_step": (ctx.graph_launch_count() - g0) / args.steps,
                    "kernel_launches_per_step": (ctx.launch_count() - l0) / args.steps, "tuning": tuning},
         "mse_vs_fp64": batch_mse(ctx, jobs[:4]) if not args.no_mse else None,
+        "cpu_baseline": None if args.no_cpu else batch_cpu_baseline(scenes, jobs, args.cpu_budget),
         "clocks": clk.summary,
     }))
     ctx.close()
+
+
+def batch_cpu_baseline(scenes, jobs, budget_s: float) -> dict:
+    """The oracle restatement of the reference on the batch's scenes in
+    order, one interleaved row set (about 4 rows per host thread, spread
+    over the image) per scene, until about budget_s of wall time."""
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    rays, done, t_total = 0, 0, 0.0
+    for (m, tree), j in zip(scenes, jobs):
+        if t_total >= budget_s:
+            break
+        nodes, tris, box = tree.export()
+        sc = orc.Scene(nodes, tris, box)
+        step = max(1, j.height // (4 * threads))
+        t0 = time.perf_counter()
+        _, st = sc.render(m.camera, m.light, j.width, j.height, j.pixel_samples, j.max_depth, seed=j.seed,
+                          threads=threads, rows=(0, j.height), row_step=step)
+        t_total += time.perf_counter() - t0
+        rays += int(st[0])
+        done += 1
+    return {"value": round(rays / t_total / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"one interleaved row set of each of the first {done} scenes ({t_total:.1f} s, oracle "
+                      f"restatement of the reference, {threads} host threads)"}
 
 
 def batch_mse(ctx, jobs, rows: int = 8, ref_spp: int = 4096) -> list:
@@ -338,6 +365,7 @@ def run_guide(args) -> None:
 
     side, depth = args.guide_side, 5
     ctx = tg.Context(0)
+    ctx.set_guide_depth(args.guide_depth)
     mesh = tg.make_scene(tg.SCENE_BAFFLE_ROOM, detail=64)
     sid = ctx.upload_tree(tg.KDTree.from_mesh(mesh))
 
@@ -368,21 +396,27 @@ def run_guide(args) -> None:
         return float(((img[..., :3] - ref[..., :3]) ** 2).mean())
 
     def run(sampling, seed, guide=None):
+        # passes of pass_spp samples accumulate on the device (no copy back
+        # per pass) until the budget is spent; the learned tracer trains on
+        # its passes for the first train_fraction of the budget
         if guide is not None:
             ctx.set_guide(guide, train=False)
-        ctx.accumulate(job(sampling, args.pass_spp, seed), 1)   # warm-up pass (workspace), not trained on
+        ctx.accumulate(job(sampling, args.pass_spp, seed), 1, readback=False)   # warm-up pass (workspace)
         if guide is not None:
             ctx.set_guide(guide, train=True, lr=args.guide_lr, records=args.guide_records,
                           steps_per_pass=args.guide_steps)
-        t = time.perf_counter()
-        img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1)
         training = guide is not None
-        while time.perf_counter() - t < args.budget:
+        t = time.perf_counter()
+        while True:
             if training and time.perf_counter() - t > args.train_fraction * args.budget:
                 ctx.set_guide(guide, train=False)   # the rest of the budget renders with the trained network
                 training = False
-            img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1 if training else 4)
-        return img, total, time.perf_counter() - t
+            ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1, readback=False)
+            if time.perf_counter() - t >= args.budget:
+                break
+        wall = time.perf_counter() - t
+        img, total = ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 0)   # read the mean back
+        return img, total, wall
 
     reps = []
     with Clocks(0) as clk:
@@ -413,7 +447,7 @@ def run_guide(args) -> None:
                    "reference_spp": int(ref_spp), "reference_s": round(ref_s, 2), "budget_s": args.budget,
                    "pass_spp": args.pass_spp, "train_fraction": args.train_fraction,
                    "records_per_pass": args.guide_records, "steps_per_pass": args.guide_steps,
-                   "lr": args.guide_lr, "repeats": args.guide_repeats},
+                   "lr": args.guide_lr, "repeats": args.guide_repeats, "guide_depth": args.guide_depth},
         "repeats": reps,
         "clocks": clk.summary,
     }))
@@ -601,10 +635,11 @@ def main() -> None:
     ap.add_argument("--budget", type=float, default=10.0)
     ap.add_argument("--ref-cache", default="", help="guide: .npz file that keeps the FP64 reference between runs")
     ap.add_argument("--train-fraction", type=float, default=0.2)
-    ap.add_argument("--guide-records", type=int, default=1 << 16)
+    ap.add_argument("--guide-records", type=int, default=1 << 18)
     ap.add_argument("--guide-lr", type=float, default=1e-3)
     ap.add_argument("--guide-steps", type=int, default=16, help="Adam steps per training pass")
     ap.add_argument("--guide-repeats", type=int, default=3, help="guide: independent seeds (fresh networks)")
+    ap.add_argument("--guide-depth", type=int, default=64, help="guided sampling at hits of depth < this")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")

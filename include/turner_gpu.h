@@ -366,7 +366,9 @@ uint64_t turner_graph_launch_count(turner_ctx* ctx);
 /* Progressive FP64 accumulation for converged reference images: adds
  * `passes` further sample passes of pixel_samples each to a double-precision
  * per-pixel sum held by the context (keyed by job seed and size) and writes
- * the running mean (linear radiance, no tone map) to out_rgba. */
+ * the running mean (linear radiance, no tone map) to out_rgba_mean. With
+ * out_rgba_mean NULL the sum stays on the device (nothing is copied back;
+ * a later call with passes = 0 reads the mean). */
 int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t passes, double* out_rgba_mean,
                              uint64_t* total_samples, uint32_t flags);
 
@@ -405,6 +407,10 @@ int turner_guide_train(turner_guide* guide, const float* features, const float* 
  * learning rate lr runs, on the context's stream without a host
  * synchronisation. Training renders are not captured into graphs. */
 int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, uint32_t records_per_pass);
+/* Guided jobs sample from the proposal at hits of depth < depth (1..64,
+ * default 64: every bounce) and by cosine below; network inputs and
+ * inference run only for the guided depths. No reference counterpart. */
+int turner_set_guide_depth(turner_ctx* ctx, uint32_t depth);
 /* Adam steps per training pass (1..64, default 16), each over all of the
  * pass's records: more steps per pass learn faster from the same samples
  * (16 gave the best equal-time result on the baffled room; each step takes

@@ -90,3 +90,49 @@ def test_failed_rank_is_reported_not_hung(tmp_path):
     # rank 0 waited in the gather and was released by the timeout with an error
     assert (tmp_path / "rank0.err").exists()
     assert not (tmp_path / "rank0.npy").exists()
+
+
+def _gpu_worker(rank, world, port, out_dir):
+    import torch.distributed as dist
+
+    import turner_gb300 as tg
+    from turner_gb300.shard import gather_rows
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=60))
+    try:
+        m = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=3)
+        with tg.Context(0) as ctx:
+            sid = ctx.upload_tree(tg.KDTree.from_mesh(m))
+            y0, y1 = row_range(GH, rank, world)
+            job = tg.make_job(sid, m, GW, GH, pixel_samples=SPP, max_depth=DEPTH, seed=SEED, rows=(y0, y1))
+            (img,), _ = ctx.render([job])
+        full = gather_rows(img, GH)
+        np.save(os.path.join(out_dir, f"gpu_rank{rank}.npy"), full)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+GW, GH = 40, 27
+
+
+@pytest.mark.gpu
+def test_two_ranks_render_their_rows_on_the_gpu(tmp_path):
+    """The product path of the row partition: two ranks (processes, gloo on
+    the host) each render their rows through turner_render's row range and
+    all-gather them; the frame equals one single-process GPU render bit for
+    bit. Both ranks share one GPU; their kernels never wait on each other
+    (only the host-side gather does)."""
+    import turner_gb300 as tg
+
+    port = _free_port()
+    mp.spawn(_gpu_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    m = tg.make_scene(tg.SCENE_SPHERE_ROOM, detail=3)
+    with tg.Context(0) as ctx:
+        sid = ctx.upload_tree(tg.KDTree.from_mesh(m))
+        (ref,), _ = ctx.render([tg.make_job(sid, m, GW, GH, pixel_samples=SPP, max_depth=DEPTH, seed=SEED)])
+    for r in range(2):
+        got = np.load(tmp_path / f"gpu_rank{r}.npy")
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))

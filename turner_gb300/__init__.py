@@ -145,6 +145,7 @@ def _lib() -> C.CDLL:
         "turner_guide_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
         "turner_set_guide": (C.c_int, [_P, _P, C.c_int, C.c_float, C.c_uint32]),
         "turner_set_guide_steps": (C.c_int, [_P, C.c_uint32]),
+        "turner_set_guide_depth": (C.c_int, [_P, C.c_uint32]),
         "turner_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
         "turner_guide_destroy": (None, [_P]),
         "turner_guide_params": (C.c_int, [_P, _P, C.c_int]),
@@ -196,8 +197,8 @@ def _check(status: int, what: str) -> None:
         raise TurnerError(status, what)
 
 
-def _ptr(a: np.ndarray) -> int:
-    return a.ctypes.data
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
 
 
 # ------------------------------------------------------------------ scenes
@@ -525,14 +526,19 @@ class Context:
     def graph_launch_count(self) -> int:
         return _lib().turner_graph_launch_count(self._h)
 
-    def accumulate(self, job: Job, passes: int) -> tuple[np.ndarray, int]:
+    def accumulate(self, job: Job, passes: int, readback: bool = True) -> tuple[np.ndarray | None, int]:
         """FP64 running mean of linear radiance after `passes` more passes of
-        job.pixel_samples samples each: ((h, w, 4) float64, total samples)."""
-        out = np.empty((max(0, job.rows), job.width, 4), np.float64)
+        job.pixel_samples samples each: ((h, w, 4) float64, total samples).
+        readback=False keeps the sum on the device and returns (None, total)."""
+        out = np.empty((max(0, job.rows), job.width, 4), np.float64) if readback else None
         total = C.c_uint64(0)
         _check(_lib().turner_render_accumulate(self._h, C.byref(job), passes, _ptr(out), C.byref(total),
                                                HOST_BUFFERS), "turner_render_accumulate")
         return out, total.value
+
+    def set_guide_depth(self, depth: int) -> None:
+        """Guided jobs sample from the proposal at hits of depth < depth."""
+        _check(_lib().turner_set_guide_depth(self._h, depth), "turner_set_guide_depth")
 
     def render(self, jobs: list[Job], outs: list[int] | None = None, flags: int = HOST_BUFFERS):
         """Renders jobs; returns (images, stats). With flags=DEVICE_BUFFERS,

@@ -100,6 +100,7 @@ struct turner_ctx {
     float guide_lr = 1e-3f;
     uint32_t guide_records = 1u << 18;   // training samples per pass
     uint32_t guide_steps_per_pass = 16;   // Adam steps on each pass's samples
+    int32_t guide_depth = 64;             // hits below this depth sample by cosine
     DevBuf gfeat, gout, qa_rec, qb_rec, r_feat, r_dir, r_weight, r_path, r_lbefore, r_tafter, r_fcp, r_count;
     double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
@@ -672,6 +673,7 @@ int plan_batch(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, float4*
         fill_job(jobs[j], ctx->scenes[jobs[j].scene_id]->view, b.table[j]);
         JobDesc& d = b.table[j];
         d.tone_map = tone_map ? 1 : 0;
+        d.guide_depth = ctx->guide_depth;
         d.pixel_offset = pixels;
         d.path_offset = paths;
         d.out = outs ? outs[j] : nullptr;
@@ -789,7 +791,7 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
         cur.count = cnt;
         if (train) {
             // keep about guide_records of this pass's bounces, spread over all paths
-            const double bounces = double(c.n_paths) * std::max(1, b.levels - 1);
+            const double bounces = double(c.n_paths) * std::max(1, std::min(b.levels - 1, ctx->guide_depth));
             recs.keep = static_cast<uint32_t>(std::min(16777216.0, 16777216.0 * ctx->guide_records / bounces));
             TURNER_CK(cudaMemsetAsync(recs.count, 0, sizeof(uint32_t), ctx->stream));
         }
@@ -811,7 +813,7 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
                 KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
                 launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_rays, fast, trace_cfg, ctx->stream);
             }
-            if (b.guided && depth + 1 < b.levels) {
+            if (b.guided && depth + 1 < b.levels && depth < ctx->guide_depth) {
                 {
                     KernelTimer kt(ctx, TURNER_KERNEL_GUIDE_FEATURES);
                     launch_guide_features(jobs, depth, cur, ctx->hits.as<Hit>(), gq.feat, c.n_paths, ctx->stream);
@@ -980,7 +982,7 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
 
 int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t passes, double* out_rgba_mean,
                              uint64_t* total_samples, uint32_t flags) {
-    if (!ctx || !job || !out_rgba_mean || flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
+    if (!ctx || !job || flags > TURNER_DEVICE_BUFFERS) return TURNER_ERR_INVALID_ARG;
     int st = check_job(ctx, *job);
     if (st != TURNER_OK) return st;
     TURNER_CK(cudaSetDevice(ctx->device));
@@ -1009,6 +1011,10 @@ int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t pa
         if (st != TURNER_OK) return st;
         ctx->acc_passes += 1;
         ctx->acc_samples += job->pixel_samples;
+    }
+    if (!out_rgba_mean) {   // the sum stays on the device
+        if (total_samples) *total_samples = ctx->acc_samples;
+        return TURNER_OK;
     }
     std::vector<double> sums(4 * n);
     TURNER_CK(cudaMemcpyAsync(sums.data(), ctx->acc.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
@@ -1238,6 +1244,12 @@ int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, 
     ctx->guide_train = train != 0 && guide;
     ctx->guide_lr = lr;
     if (records_per_pass) ctx->guide_records = records_per_pass;
+    return TURNER_OK;
+}
+
+int turner_set_guide_depth(turner_ctx* ctx, uint32_t depth) {
+    if (!ctx || depth < 1 || depth > 64) return TURNER_ERR_INVALID_ARG;
+    ctx->guide_depth = static_cast<int32_t>(depth);
     return TURNER_OK;
 }
 

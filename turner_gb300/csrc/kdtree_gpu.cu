@@ -523,21 +523,24 @@ __global__ void __launch_bounds__(kMidThreads) k_level_mid(const Cell* __restric
                 if (lo == hi) s_pl[atomicAdd(&n_pl, 1u)] = lo;
             }
             __syncthreads();
+            // the boxes that were written: the same as the kept ones whenever
+            // clipping gives lo <= hi on axis 0 (na <= n <= len in any case)
+            const uint32_t na = n_axis;
             const uint32_t npl = n_pl;
-            for (uint32_t i = n + tid; i < len; i += kMidThreads) {
+            for (uint32_t i = na + tid; i < len; i += kMidThreads) {
                 s_lo[i] = INFINITY;
                 s_hi[i] = INFINITY;
             }
             for (uint32_t i = npl + tid; i < len; i += kMidThreads) s_pl[i] = INFINITY;
             __syncthreads();
             bitonic_sort3(s_lo, s_hi, s_pl, len);
-            for (uint32_t t = tid; t < 2 * n; t += kMidThreads) {
-                const float pos = t < n ? s_lo[t] : s_hi[t - n];
+            for (uint32_t t = tid; t < 2 * na; t += kMidThreads) {
+                const float pos = t < na ? s_lo[t] : s_hi[t - na];
                 if (!(pos >= c.lo[a] && pos <= c.hi[a])) continue;
-                const uint32_t nl = count_below(s_lo, n, pos);
-                const uint32_t nr = n - count_not_above(s_hi, n, pos);
+                const uint32_t nl = count_below(s_lo, na, pos);
+                const uint32_t nr = na - count_not_above(s_hi, na, pos);
                 const uint32_t np = count_not_above(s_pl, npl, pos) - count_below(s_pl, npl, pos);
-                consider(c, sa, n, a, pos, nl, nr, np, bc, ba, bp, bpl, bnl, bnr);
+                consider(c, sa, na, a, pos, nl, nr, np, bc, ba, bp, bpl, bnl, bnr);
             }
             __syncthreads();   // the next axis refills the arrays
         }

@@ -72,6 +72,7 @@ struct JobDesc {
     float light_pos[3];
     float light_col[4];
     int32_t sampling, traversal;
+    int32_t guide_depth;     // guided jobs: hits at depth < guide_depth sample from the proposal, deeper ones by cosine
     float exposure, inv_gamma;
     int32_t gamma, tone_map;
     int32_t renderer;

@@ -166,7 +166,8 @@ __global__ void __launch_bounds__(kBlock) k_guide_features(const JobDesc* __rest
         const float4 d4 = q.d[i];
         const JobDesc& job = jobs[__float_as_uint(d4.w)];
         const Hit h = hits[i];
-        if (job.sampling == kSamplingGuided && depth < job.max_depth && job.mc > 0 && h.id < kMiss) {
+        if (job.sampling == kSamplingGuided && depth < job.guide_depth && depth < job.max_depth && job.mc > 0 &&
+            h.id < kMiss) {
             const float4 o4 = q.o[i];
             const float3 p = make_float3(o4.x + h.r * d4.x, o4.y + h.r * d4.y, o4.z + h.r * d4.z);
             const float4* rec = job.sc.shade + 4 * size_t(h.id);
@@ -281,7 +282,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                     float x, y, z, weight;
                     float3 dir;
                     bool bounce = true;
-                    if (job.sampling == kSamplingGuided) {
+                    // guided jobs sample from the proposal up to guide_depth, by cosine below
+                    const bool guided = job.sampling == kSamplingGuided && depth < job.guide_depth;
+                    if (guided) {
                         // learned proposal: 1/2 cosine about the normal, 1/2 the vMF mixture
                         float raw[guide::kOut];
 #pragma unroll
@@ -340,7 +343,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                         y = rr * sinf(phi);
                         weight = 1.f;
                     }
-                    if (job.sampling != kSamplingGuided) {
+                    if (!guided) {
                         dir = make_float3(m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z,
                                           m[6] * x + m[7] * y + m[8] * z);
                     }
