@@ -224,6 +224,14 @@ int turner_probe_gather(turner_ctx* ctx, uint64_t buffer_bytes, uint32_t load_by
 #define TURNER_RAYS_INTERSECT 4       /* turner_intersect and turner_occluded   */
 #define TURNER_RAYS_KINDS 5
 int turner_set_traversal_refill(turner_ctx* ctx, int kind, uint32_t lanes);
+/* Where the persistent traversal keeps its stack: entries = 4 or 8 puts each
+ * thread's newest entries in shared memory ([slot][thread] words, so lanes
+ * at different depths never share a bank) and moves older ones to local
+ * memory; 0 (default) keeps the whole stack in local memory. Applies to the
+ * default launch shape (128-thread blocks, 10 per SM, no mailbox). Results
+ * do not depend on it. No reference counterpart: the reference's stack is a
+ * heap std::stack (lib/kdtree.cpp:522-560). */
+int turner_set_traversal_ring(turner_ctx* ctx, uint32_t entries);
 
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the

@@ -139,6 +139,7 @@ def test_refill_thresholds_are_invisible(ctx):
         for lanes in (1, 7, 32):
             for k in kinds:
                 ctx.set_traversal_refill(k, lanes)
+            ctx.set_traversal_ring(8 if lanes == 7 else 0)
             (b,), (sb,) = ctx.render([job])
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and sa.rays == sb.rays
             h2 = ctx.intersect(sid, o, d)
@@ -146,6 +147,7 @@ def test_refill_thresholds_are_invisible(ctx):
         with pytest.raises(tg.TurnerError):
             ctx.set_traversal_refill(tg.RAYS_BOUNCE, 33)
     finally:
+        ctx.set_traversal_ring(0)
         for k, v in zip(kinds, defaults):
             ctx.set_traversal_refill(k, v)
 

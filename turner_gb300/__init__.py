@@ -131,6 +131,7 @@ def _lib() -> C.CDLL:
         "turner_graph_launch_count": (C.c_uint64, [_P]),
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_set_traversal_refill": (C.c_int, [_P, C.c_int, C.c_uint32]),
+        "turner_set_traversal_ring": (C.c_int, [_P, C.c_uint32]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
@@ -428,6 +429,11 @@ class Context:
         """A warp of the persistent traversal takes new rays of this kind
         (RAYS_*) only once `lanes` of its lanes are idle."""
         _check(_lib().turner_set_traversal_refill(self._h, kind, lanes), "turner_set_traversal_refill")
+
+    def set_traversal_ring(self, entries: int) -> None:
+        """0, 4 or 8: how many of each thread's newest traversal-stack entries
+        live in shared memory (the rest in local memory)."""
+        _check(_lib().turner_set_traversal_ring(self._h, entries), "turner_set_traversal_ring")
 
     def set_profiling(self, on: bool) -> None:
         _check(_lib().turner_set_profiling(self._h, 1 if on else 0), "turner_set_profiling")

@@ -135,8 +135,54 @@ __device__ __forceinline__ float pick(float3 v, uint32_t ax) { return ax == 0 ? 
 template <int N>
 struct LocalStack {
     uint2 e[N];
+    __device__ __forceinline__ void reset() {}
     __device__ __forceinline__ void put(int k, uint2 v) { e[k] = v; }
     __device__ __forceinline__ uint2 get(int k) const { return e[k]; }
+};
+
+// A stack whose newest R entries live in shared memory, the older ones in
+// local memory. Shared memory holds two words per entry, [slot][thread] for
+// the far child and the exit distance, so lanes at different depths of their
+// own stacks never conflict on a bank (word = slot * BLOCK + thread): a
+// divergent push or pop is one shared-memory wavefront per word, where the
+// same access to local memory touches up to 32 cache lines. A push onto a
+// full ring first moves the oldest ring entry to local memory; a pop from an
+// empty ring takes the entry from local memory. Entries stay in push order,
+// so pops return exactly what LocalStack would.
+template <int R, int BLOCK, int N>
+struct RingStack {
+    static_assert((R & (R - 1)) == 0, "ring size is a power of two");
+    uint2 spill[N];    // entries below `base`
+    int base;          // entries [base, sp) are in the ring
+    // the block's dynamic shared memory: [R][BLOCK] far-child words, then
+    // [R][BLOCK] exit-distance words (addresses recomputed per access, so no
+    // register holds a pointer)
+    __device__ __forceinline__ static uint32_t* words() {
+        extern __shared__ uint32_t ring_smem[];
+        return ring_smem;
+    }
+    __device__ __forceinline__ void init() { base = 0; }
+    __device__ __forceinline__ void reset() { base = 0; }
+    __device__ __forceinline__ void put(int k, uint2 v) {
+        uint32_t* w = words();
+        if (k - base >= R) {   // the ring is full: its oldest entry (slot of base) goes to local memory
+            const int o = (base & (R - 1)) * BLOCK + static_cast<int>(threadIdx.x);
+            spill[base] = make_uint2(w[o], w[R * BLOCK + o]);
+            ++base;
+        }
+        const int s = (k & (R - 1)) * BLOCK + static_cast<int>(threadIdx.x);
+        w[s] = v.x;
+        w[R * BLOCK + s] = v.y;
+    }
+    __device__ __forceinline__ uint2 get(int k) {
+        if (k < base) {   // the ring is empty: the entry is in local memory
+            base = k;
+            return spill[k];
+        }
+        const uint32_t* w = words();
+        const int s = (k & (R - 1)) * BLOCK + static_cast<int>(threadIdx.x);
+        return make_uint2(w[s], w[R * BLOCK + s]);
+    }
 };
 
 // KDTreeIntersection::intersect (lib/kdtree.cpp:516-607).

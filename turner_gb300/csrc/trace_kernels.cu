@@ -706,6 +706,7 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
                         if (in_box) {
                             cur = idx;
                             active = true;
+                            st.reset();
                         } else {
                             src.store(idx, s.best);   // misses the scene box
                         }
@@ -725,19 +726,32 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
 // __launch_bounds__ changes ptxas's register budget (61 instead of 56
 // registers for the closest-hit kernel, 8 instead of 9 resident blocks), so
 // the uncapped kernel gives only the block size.
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX>
-__global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
-                                                     uint32_t* __restrict__ work, uint32_t refill) {
-    LocalStack<STACK> st;
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
+// RING > 0: the stack's newest RING entries in shared memory (RingStack,
+// 8 * RING bytes per thread of dynamic shared memory), else all in local memory.
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int RING>
+__device__ __forceinline__ void traverse_body(const SceneView& single, const JobDesc* __restrict__ jobs, Src& src,
+                                              uint32_t* __restrict__ work, uint32_t refill) {
+    if constexpr (RING > 0) {
+        RingStack<RING, BLOCK, STACK> st;
+        st.init();
+        traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
+    } else {
+        LocalStack<STACK> st;
+        traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
+    }
 }
 
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int RING>
+__global__ void __launch_bounds__(BLOCK) k_traverse(SceneView single, const JobDesc* __restrict__ jobs, Src src,
+                                                     uint32_t* __restrict__ work, uint32_t refill) {
+    traverse_body<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, RING>(single, jobs, src, work, refill);
+}
+
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB, int RING>
 __global__ void __launch_bounds__(BLOCK, MINB) k_traverse_capped(SceneView single, const JobDesc* __restrict__ jobs,
                                                                   Src src, uint32_t* __restrict__ work,
                                                                   uint32_t refill) {
-    LocalStack<STACK> st;
-    traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
+    traverse_body<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, RING>(single, jobs, src, work, refill);
 }
 
 // Per-pixel mean in sample order, exposure (1 - exp(-x e)) and gamma (x^g)
@@ -792,7 +806,7 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(const JobDesc* __restrict
 inline unsigned grid_for(uint64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
 // Resident blocks per SM x SMs for a persistent kernel (cached per kernel).
-template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap) {
+template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks_per_sm_cap, size_t dyn_smem = 0) {
     // resident blocks per SM, per kernel (kernels that share a signature
     // differ in registers) and per device
     static std::mutex mu;
@@ -807,7 +821,7 @@ template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks
         if (it == cache.end()) {
             int sms = 0, per_sm = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, dyn_smem);
             it = cache.emplace(key, std::make_pair(std::max(1, sms), std::max(1, per_sm))).first;
         }
         v = it->second;
@@ -816,15 +830,16 @@ template <int BLOCK, class K> unsigned persistent_grid(K kernel, unsigned blocks
     return static_cast<unsigned>(v.first) * per;
 }
 
-template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB>
+template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int MINB, int RING = 0>
 void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src& src, uint32_t capacity,
                         const TraverseCfg& cfg, cudaStream_t stream) {
     void (*kernel)(SceneView, const JobDesc*, Src, uint32_t*, uint32_t);
-    if constexpr (MINB > 1) kernel = k_traverse_capped<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB>;
-    else kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX>;
+    if constexpr (MINB > 1) kernel = k_traverse_capped<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB, RING>;
+    else kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, RING>;
+    const size_t smem = size_t(RING) * 2 * sizeof(uint32_t) * BLOCK;
     const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
-    const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm), std::max(1u, need));
-    kernel<<<grid, BLOCK, 0, stream>>>(single, jobs, src, cfg.work, std::max(1u, std::min(32u, cfg.refill)));
+    const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm, smem), std::max(1u, need));
+    kernel<<<grid, BLOCK, smem, stream>>>(single, jobs, src, cfg.work, std::max(1u, std::min(32u, cfg.refill)));
 }
 
 // Dispatch on the tuned block size and stack depth. The stack must hold the
@@ -852,6 +867,14 @@ void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, 
     case 12: TURNER_SHAPE(ST, MB, 12); break;             \
     case 16: TURNER_SHAPE(ST, MB, 16); break;             \
     default: TURNER_SHAPE(ST, MB, 1); break;              \
+    }
+    if (cfg.ring && !cfg.mailbox && cfg.min_blocks == 10) {
+        // the stack's newest 4 or 8 entries in shared memory
+        if (cfg.ring == 4) run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap, false, 10, 4>(single, jobs, src,
+                                                                                                 capacity, cfg, stream);
+        else run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap, false, 10, 8>(single, jobs, src, capacity, cfg,
+                                                                                     stream);
+        return;
     }
     if (small_stack) {
         if (cfg.mailbox) { TURNER_CAPS(64, true) } else { TURNER_CAPS(64, false) }
