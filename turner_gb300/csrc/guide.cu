@@ -81,13 +81,25 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 
 // Eight encoded inputs k = 8g .. 8g + 7 of one sample (see encode()): groups
 // 0-8 are four frequencies of one axis, group 9 the normal, albedo and padding.
+// The group's first frequency comes from sincospif, the next three from the
+// double-angle identities sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)
+// (cos a + sin a): three doublings grow the FP32 error by at most 8x, far
+// below the BF16 rounding of the stored value (2^-9).
 __device__ __forceinline__ uint4 encode_group(int g, const float p[3], const float nn[3], const float a[3]) {
     float f[8];
     if (g < 9) {
         const int ax = g / 3, i0 = (g - ax * 3) * 4;
         const float x = g < 3 ? p[0] : g < 6 ? p[1] : p[2];
+        float sn, cs;
+        sincospif(x * static_cast<float>(1 << i0), &sn, &cs);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) sincospif(x * static_cast<float>(1 << (i0 + j)), &f[2 * j], &f[2 * j + 1]);
+        for (int j = 0; j < 4; ++j) {
+            f[2 * j] = sn;
+            f[2 * j + 1] = cs;
+            const float s2 = 2.f * sn * cs;
+            cs = (cs - sn) * (cs + sn);
+            sn = s2;
+        }
     } else {
         f[0] = nn[0]; f[1] = nn[1]; f[2] = nn[2];
         f[3] = a[0]; f[4] = a[1]; f[5] = a[2];
@@ -151,7 +163,8 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
         }
     };
     load_features(blockIdx.x);
-    for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
+    bool aborted = false;   // the same in every thread: set after a barrier
+    for (uint32_t tile = blockIdx.x; tile < tiles && !aborted; tile += gridDim.x) {
         const uint32_t s = tile * 128 + row;
         const bool valid = s < n;
         uint4* const act_row = acts && valid ? reinterpret_cast<uint4*>(acts + size_t(s) * 336) : nullptr;
@@ -176,21 +189,25 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
         for (int l = 0; l < kLayers; ++l) {
             const int K = layer_in(l), N = layer_out_pad(l);
             if (tid == 0) issue_layer(tmem, sm.act, sm.w + fwd_off(l), K, N, &sm.mbar);
-            if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
+            // a wait that gives up still runs the epilogue (on whatever TMEM
+            // holds); the barrier at the end of the layer then aborts the
+            // whole CTA together
+            const bool timed_out = !tc::mbar_wait(&sm.mbar, phase, err);
             phase ^= 1;
             tc::tc_fence_after_sync();
-            __syncthreads();
-            if (sm.abort) break;
             const uint32_t c0 = static_cast<uint32_t>(half * 32);
             if (l < kLayers - 1) {
                 float v[32];
                 tc::tmem_ld16(tmem + lane_base + c0, v);
                 tc::tmem_ld16(tmem + lane_base + c0 + 16u, v + 16);
+                const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
+                    const float4 ba = b4[2 * q], bb = b4[2 * q + 1];
+                    const float bq[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
                     float y[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) y[j] = fmaxf(v[8 * q + j] + sm.bias[bias_o + c0 + 8 * q + j], 0.f);
+                    for (int j = 0; j < 8; ++j) y[j] = fmaxf(v[8 * q + j] + bq[j], 0.f);
                     const uint4 u = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]),
                                                pack_bf16x2(y[4], y[5]), pack_bf16x2(y[6], y[7]));
                     *reinterpret_cast<uint4*>(sm.act + tc::kmajor_offset(row, c0 + 8 * q, kHidden)) = u;
@@ -226,11 +243,15 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
             bias_o += layer_out(l);
             tc::fence_async_smem();
             tc::tc_fence_before_sync();
-            __syncthreads();
+            const int any_timeout = __syncthreads_or(timed_out ? 1 : 0);
             tc::tc_fence_after_sync();
+            if (any_timeout) {
+                aborted = true;
+                break;
+            }
         }
     }
-    if (sm.abort && tid == 0) {
+    if (aborted && tid == 0) {
         // drain: an MMA may still be in flight; wait once more (bounded)
         tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
     }
