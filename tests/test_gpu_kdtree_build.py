@@ -115,3 +115,58 @@ def test_gpu_build_rejects_bad_input(ctx):
     with pytest.raises(tg.TurnerError):
         tg.KDTree.build_gpu(ctx, tg.Mesh(np.zeros((0, 9), np.float32), np.zeros((0, 9), np.float32),
                                          np.zeros((0, 4), np.float32), tg.Camera(), 0.5, None))
+
+
+def exact_sah_costs(lo, hi, cell_lo, cell_hi):
+    """Every candidate plane of a cell whose references have the clipped boxes
+    lo, hi (n x 3), swept exactly in FP64: [(cost, axis, position)] under the
+    GPU build's rules (nl = boxes starting before the plane, nr = ending after
+    it, boxes lying in the plane on the cheaper side, no empty-space cut, no
+    cut that leaves the cell whole; traversal cost 15, intersection cost 20)."""
+    n = lo.shape[0]
+    ext = cell_hi - cell_lo
+    sa = 2 * (ext[0] * ext[1] + ext[0] * ext[2] + ext[1] * ext[2])
+    out = []
+    for a in range(3):
+        slo, shi = np.sort(lo[:, a]), np.sort(hi[:, a])
+        flat = np.sort(lo[lo[:, a] == hi[:, a], a])
+        cand = np.unique(np.concatenate([lo[:, a], hi[:, a]]))
+        cand = cand[(cand >= cell_lo[a]) & (cand <= cell_hi[a])]
+        nl = np.searchsorted(slo, cand, side="left")
+        nr = n - np.searchsorted(shi, cand, side="right")
+        npl = np.searchsorted(flat, cand, side="right") - np.searchsorted(flat, cand, side="left")
+        o1, o2 = [q for q in range(3) if q != a]
+        for pl in (1, 0):
+            l = nl + (npl if pl else 0)
+            r = nr + (0 if pl else npl)
+            ok = ~((l == n) & (r == n)) & (l > 0) & (r > 0)
+            ok &= ~((cand == cell_lo[a]) & (r == n)) & ~((cand == cell_hi[a]) & (l == n))
+            dl = cand.astype(np.float64) - cell_lo[a]
+            dr = cell_hi[a] - cand.astype(np.float64)
+            sl = 2 * (dl * ext[o1] + dl * ext[o2] + ext[o1] * ext[o2])
+            sr = 2 * (dr * ext[o1] + dr * ext[o2] + ext[o1] * ext[o2])
+            cost = 15 + 20 * (sl / sa * l + sr / sa * r)
+            out += [(float(cst), a, float(p)) for cst, p in zip(cost[ok], cand[ok])]
+    return out
+
+
+@pytest.mark.parametrize("count", [1500, 3000, 7000])
+def test_mid_cell_split_is_the_exact_optimum(ctx, count):
+    """A root cell of 1,025-8,192 references goes through the sorted-bounds
+    sweep (k_level_mid). Its chosen plane must be an optimum of the exact
+    O(n^2)-equivalent sweep over every clipped-box bound (here in FP64 with
+    sorted counts): the same axis and a cost within rounding of the best."""
+    m = tg.make_scene(tg.SCENE_SOUP, count=count, seed=31)
+    assert 1024 < m.n_triangles <= 8192
+    nodes, _, box = tg.KDTree.build_gpu(ctx, m).export()
+    v = m.vertices.reshape(-1, 3, 3).astype(np.float64)
+    lo, hi = v.min(axis=1), v.max(axis=1)
+    root = int(nodes[0])
+    assert root & 3 != 3, "the root must be split"
+    axis = root & 3
+    pos = np.array([root >> 32], np.uint32).view(np.float32)[0]
+    costs = exact_sah_costs(lo, hi, box[:3].astype(np.float64), box[3:].astype(np.float64))
+    best = min(c for c, _, _ in costs)
+    mine = [c for c, a, p in costs if a == axis and p == float(pos)]
+    assert mine, f"plane {pos} on axis {axis} is not a candidate"
+    assert min(mine) <= best * (1 + 1e-5), (min(mine), best)
