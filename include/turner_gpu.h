@@ -232,6 +232,14 @@ int turner_set_traversal_refill(turner_ctx* ctx, int kind, uint32_t lanes);
  * do not depend on it. No reference counterpart: the reference's stack is a
  * heap std::stack (lib/kdtree.cpp:522-560). */
 int turner_set_traversal_ring(turner_ctx* ctx, uint32_t entries);
+/* on != 0: speculative traversal rounds (Aila & Laine 2009): a lane that has
+ * found a leaf sets its triangle run aside and descends on toward the next
+ * leaf while other lanes of its warp are still searching, then the warp tests
+ * the runs set aside together. Leaf runs are still tested in the reference's
+ * order, so results do not change. Applies to the default launch shape and
+ * PARITY / shadow traversal (not FAST). Default off. No reference
+ * counterpart: tuning knob of this library. */
+int turner_set_traversal_speculative(turner_ctx* ctx, int on);
 
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the

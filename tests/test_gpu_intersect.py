@@ -223,23 +223,31 @@ def test_full_hit_test_set(ctx, sphere_room_327k):
     assert np.array_equal(fast[0], cpu[0])
 
 
-@pytest.mark.parametrize("ring", [4, 8])
+@pytest.mark.parametrize("ring", [4, 8, "speculative"])
 def test_shared_memory_stack_is_exact(ctx, uploaded, ring):
     """The traversal stack with its newest 4 or 8 entries in shared memory
-    and older ones in local memory: identical hits, for closest-hit and
-    shadow (any-hit) traversal, on trees much deeper than the ring."""
+    and older ones in local memory, and speculative traversal rounds:
+    identical hits, for closest-hit and shadow (any-hit) traversal, on trees
+    much deeper than the ring."""
+    def setting(on):
+        if ring == "speculative":
+            ctx.set_traversal_speculative(on)
+        else:
+            ctx.set_traversal_ring(ring if on else 0)
+
     for name in ("sphere5", "baffle32", "soup20k"):
         sid, ref, box = uploaded[name]
         o, d = tg.make_rays(100_000, box, seed=23)
         tm = np.random.default_rng(3).uniform(0, 6, o.shape[1]).astype(np.float32)
         base = ctx.intersect(sid, o, d)
         occ = ctx.occluded(sid, o, d, tm)
-        ctx.set_traversal_ring(ring)
+        assert_same(base, ref.intersect(o, d))
+        setting(True)
         try:
             got = ctx.intersect(sid, o, d)
             occ2 = ctx.occluded(sid, o, d, tm)
         finally:
-            ctx.set_traversal_ring(0)
+            setting(False)
         assert_same(got, base)
         assert np.array_equal(occ, occ2)
     with pytest.raises(tg.TurnerError):

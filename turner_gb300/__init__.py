@@ -132,6 +132,7 @@ def _lib() -> C.CDLL:
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_set_traversal_refill": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_set_traversal_ring": (C.c_int, [_P, C.c_uint32]),
+        "turner_set_traversal_speculative": (C.c_int, [_P, C.c_int]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
@@ -429,6 +430,10 @@ class Context:
         """A warp of the persistent traversal takes new rays of this kind
         (RAYS_*) only once `lanes` of its lanes are idle."""
         _check(_lib().turner_set_traversal_refill(self._h, kind, lanes), "turner_set_traversal_refill")
+
+    def set_traversal_speculative(self, on: bool) -> None:
+        """Speculative traversal rounds (same results)."""
+        _check(_lib().turner_set_traversal_speculative(self._h, 1 if on else 0), "turner_set_traversal_speculative")
 
     def set_traversal_ring(self, entries: int) -> None:
         """0, 4 or 8: how many of each thread's newest traversal-stack entries

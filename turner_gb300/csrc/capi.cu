@@ -630,6 +630,12 @@ int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths) {
     return TURNER_OK;
 }
 
+int turner_set_traversal_speculative(turner_ctx* ctx, int on) {
+    if (!ctx) return TURNER_ERR_INVALID_ARG;
+    ctx->traverse.speculative = on != 0;
+    return TURNER_OK;
+}
+
 int turner_set_traversal_ring(turner_ctx* ctx, uint32_t entries) {
     if (!ctx || (entries != 0 && entries != 4 && entries != 8)) return TURNER_ERR_INVALID_ARG;
     ctx->traverse.ring = entries;

@@ -410,6 +410,119 @@ __device__ __forceinline__ bool trav_round(TravState& s, float tmax, Stack& st) 
     return false;
 }
 
+// Speculative form of trav_round (Aila & Laine 2009), called by all 32 lanes
+// of a warp together (`live`: the lane holds a ray). A lane that reaches a
+// leaf keeps its run aside, pops the next cell and descends on toward the
+// next leaf while some lane of its warp has not found a leaf yet; it stops at
+// that second leaf, which starts its next round. Then every lane tests the
+// run it kept. Each ray still tests its leaf runs in the reference's order
+// (the run kept aside before the one found after it), with the same bounds,
+// so the answers are those of trav_round; only FAST_EXIT's early stop is not
+// available here. s.node == kNoNode: the ray has no cell left. Returns true
+// when the lane's ray is finished.
+constexpr uint32_t kNoNode = 0xFFFFFFFFu;
+
+template <bool ANY, bool MAILBOX, class Stack>
+__device__ __forceinline__ bool trav_round_spec(TravState& s, bool live, float tmax, Stack& st) {
+    const uint2* __restrict__ nodes = s.nodes;
+    uint32_t node = s.node;
+    float tenter = s.tenter, texit = s.texit;
+    int sp = s.sp;
+    uint32_t kept = kNoNode;   // first word of the leaf run set aside
+    bool stepping = live && node != kNoNode;
+    uint2 w = make_uint2(0u, 0u);
+    if (stepping) w = __ldg(nodes + node);
+    // descend while some lane of the warp has no leaf yet
+    while (__any_sync(0xFFFFFFFFu, live && kept == kNoNode && node != kNoNode)) {
+        if (stepping) {
+            if ((w.x & 3u) != 3u) {
+                const uint32_t ax = w.x & 3u;
+                const float t = (__uint_as_float(w.y) - pick(s.o, ax)) * pick(s.inv, ax);
+                uint32_t near_c = node + 1, far_c = w.x >> 2;
+                if (s.neg & (1u << ax)) {
+                    const uint32_t tmp = near_c;
+                    near_c = far_c;
+                    far_c = tmp;
+                }
+                if (texit < t) {
+                    node = near_c;
+                } else if (t < tenter) {
+                    node = far_c;
+                } else {
+                    st.put(sp, make_uint2(far_c, __float_as_uint(texit)));
+                    ++sp;
+                    node = near_c;
+                    texit = t;
+                }
+                w = __ldg(nodes + node);
+            } else if (kept == kNoNode) {
+                // set this leaf's run aside and go on to the next cell
+                kept = node;
+                if (sp == 0) {
+                    node = kNoNode;
+                    stepping = false;
+                } else {
+                    --sp;
+                    const uint2 e = st.get(sp);
+                    node = e.x;
+                    tenter = texit;
+                    texit = __uint_as_float(e.y);
+                    w = __ldg(nodes + node);
+                }
+            } else {
+                stepping = false;   // a second leaf: it starts the next round
+            }
+        }
+    }
+    s.node = node;
+    s.tenter = tenter;
+    s.texit = texit;
+    s.sp = sp;
+    // test the runs set aside: two ids per word until a half-empty leaf or an inner node
+    bool hit_any = false;
+    bool testing = live && kept != kNoNode;
+    uint32_t wi = kept;
+    uint2 lw = make_uint2(0u, 0u);
+    if (testing) lw = __ldg(nodes + wi);
+    while (__any_sync(0xFFFFFFFFu, testing)) {
+        if (testing) {
+            const bool pair = lw.x != 0xFFFFFFFFu;
+            uint2 next = lw;
+            if (pair) next = __ldg(nodes + wi + 1);
+            float r, u, v;
+            if (!mailbox_seen<MAILBOX>(s, lw.y) &&
+                triangle_test_bounded<ANY>(s.tri, lw.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+                s.best = Hit{lw.y, r, u, v};
+                if (ANY) {
+                    hit_any = true;
+                    testing = false;
+                }
+            }
+            if (testing) {
+                if (!pair) {
+                    testing = false;
+                } else {
+                    const uint32_t id2 = lw.x >> 2;
+                    if (!mailbox_seen<MAILBOX>(s, id2) &&
+                        triangle_test_bounded<ANY>(s.tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+                        s.best = Hit{id2, r, u, v};
+                        if (ANY) {
+                            hit_any = true;
+                            testing = false;
+                        }
+                    }
+                    if (testing) {
+                        ++wi;
+                        lw = next;
+                        if ((lw.x & 3u) != 3u) testing = false;
+                    }
+                }
+            }
+        }
+    }
+    return hit_any || s.node == kNoNode;
+}
+
 // xorshift64* (lib/xorshift.h:27-70): float = (x & (2^24 - 1)) * 2^-24
 __device__ __forceinline__ float xorshift_float(uint64_t& s) {
     s ^= s >> 12;

@@ -674,7 +674,7 @@ struct OccSrc {             // turner_occluded batches: any hit with r <= tmax[i
 // neighbouring rays of a coherent queue (camera rays) stay together and share
 // node and record loads. MULTI: every ray names its job and is traced in
 // that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, class Stack>
+template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, bool SPEC = false, class Stack>
 __device__ __forceinline__ void traverse_persistent(const SceneView& single, const JobDesc* __restrict__ jobs,
                                                     Src& src, uint32_t* __restrict__ work, uint32_t refill,
                                                     Stack& st) {
@@ -715,7 +715,14 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
-        if (active && trav_round<ANY, FAST, MAILBOX>(s, tmax, st)) {
+        if constexpr (SPEC) {
+            // every lane takes part in the speculative round's warp votes
+            const bool done = trav_round_spec<ANY, MAILBOX>(s, active, tmax, st);
+            if (active && done) {
+                src.store(cur, s.best);
+                active = false;
+            }
+        } else if (active && trav_round<ANY, FAST, MAILBOX>(s, tmax, st)) {
             src.store(cur, s.best);
             active = false;
         }
@@ -728,10 +735,14 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
 // the uncapped kernel gives only the block size.
 // RING > 0: the stack's newest RING entries in shared memory (RingStack,
 // 8 * RING bytes per thread of dynamic shared memory), else all in local memory.
+// RING == -1: the local-memory stack with speculative rounds (trav_round_spec).
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int RING>
 __device__ __forceinline__ void traverse_body(const SceneView& single, const JobDesc* __restrict__ jobs, Src& src,
                                               uint32_t* __restrict__ work, uint32_t refill) {
-    if constexpr (RING > 0) {
+    if constexpr (RING < 0) {
+        LocalStack<STACK> st;
+        traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX, true>(single, jobs, src, work, refill, st);
+    } else if constexpr (RING > 0) {
         RingStack<RING, BLOCK, STACK> st;
         st.init();
         traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX>(single, jobs, src, work, refill, st);
@@ -836,7 +847,7 @@ void run_traverse_shape(const SceneView& single, const JobDesc* jobs, const Src&
     void (*kernel)(SceneView, const JobDesc*, Src, uint32_t*, uint32_t);
     if constexpr (MINB > 1) kernel = k_traverse_capped<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, MINB, RING>;
     else kernel = k_traverse<Src, ANY, FAST, MULTI, BLOCK, STACK, MAILBOX, RING>;
-    const size_t smem = size_t(RING) * 2 * sizeof(uint32_t) * BLOCK;
+    const size_t smem = RING > 0 ? size_t(RING) * 2 * sizeof(uint32_t) * BLOCK : 0;
     const unsigned need = static_cast<unsigned>((uint64_t(capacity) + BLOCK - 1) / BLOCK);
     const unsigned grid = std::min(persistent_grid<BLOCK>(kernel, cfg.blocks_per_sm, smem), std::max(1u, need));
     kernel<<<grid, BLOCK, smem, stream>>>(single, jobs, src, cfg.work, std::max(1u, std::min(32u, cfg.refill)));
@@ -867,6 +878,12 @@ void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, 
     case 12: TURNER_SHAPE(ST, MB, 12); break;             \
     case 16: TURNER_SHAPE(ST, MB, 16); break;             \
     default: TURNER_SHAPE(ST, MB, 1); break;              \
+    }
+    if (cfg.speculative && !FAST && !cfg.mailbox && cfg.min_blocks == 10) {
+        // speculative rounds (not with FAST's early stop)
+        run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap, false, 10, -1>(single, jobs, src, capacity, cfg,
+                                                                                 stream);
+        return;
     }
     if (cfg.ring && !cfg.mailbox && cfg.min_blocks == 10) {
         // the stack's newest 4 or 8 entries in shared memory
