@@ -366,6 +366,7 @@ def run_guide(args) -> None:
     side, depth = args.guide_side, 5
     ctx = tg.Context(0)
     ctx.set_guide_depth(args.guide_depth)
+    ctx.set_guide_weighting(args.guide_weighting)
     mesh = tg.make_scene(tg.SCENE_BAFFLE_ROOM, detail=64)
     sid = ctx.upload_tree(tg.KDTree.from_mesh(mesh))
 
@@ -447,7 +448,8 @@ def run_guide(args) -> None:
                    "reference_spp": int(ref_spp), "reference_s": round(ref_s, 2), "budget_s": args.budget,
                    "pass_spp": args.pass_spp, "train_fraction": args.train_fraction,
                    "records_per_pass": args.guide_records, "steps_per_pass": args.guide_steps,
-                   "lr": args.guide_lr, "repeats": args.guide_repeats, "guide_depth": args.guide_depth},
+                   "lr": args.guide_lr, "repeats": args.guide_repeats, "guide_depth": args.guide_depth,
+                   "guide_weighting": args.guide_weighting},
         "repeats": reps,
         "clocks": clk.summary,
     }))
@@ -643,6 +645,8 @@ def main() -> None:
     ap.add_argument("--guide-steps", type=int, default=16, help="Adam steps per training pass")
     ap.add_argument("--guide-repeats", type=int, default=3, help="guide: independent seeds (fresh networks)")
     ap.add_argument("--guide-depth", type=int, default=64, help="guided sampling at hits of depth < this")
+    ap.add_argument("--guide-weighting", type=int, default=0, choices=[0, 1, 2],
+                    help="training-record weights: 0 incident radiance, 1 x path throughput, 2 x its square root")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-max-tris", type=int, default=500_000)
     ap.add_argument("--autotune", action="store_true")

@@ -427,6 +427,13 @@ int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, 
  * default 64: every bounce) and by cosine below; network inputs and
  * inference run only for the guided depths. No reference counterpart. */
 int turner_set_guide_depth(turner_ctx* ctx, uint32_t depth);
+/* Weights of the online training records: 0 (default) the incident radiance
+ * times f cos / p, the target of the proposal's own distribution; 1 also
+ * times the path throughput that reached the bounce (the luminance the path
+ * gained after it), so the shared network favours the bounces that carry
+ * most of the pixels' radiance; 2 times the square root of that throughput.
+ * No reference counterpart. */
+int turner_set_guide_weighting(turner_ctx* ctx, int mode);
 /* Adam steps per training pass (1..64, default 16), each over all of the
  * pass's records: more steps per pass learn faster from the same samples
  * (16 gave the best equal-time result on the baffled room; each step takes

@@ -148,6 +148,7 @@ def _lib() -> C.CDLL:
         "turner_set_guide": (C.c_int, [_P, _P, C.c_int, C.c_float, C.c_uint32]),
         "turner_set_guide_steps": (C.c_int, [_P, C.c_uint32]),
         "turner_set_guide_depth": (C.c_int, [_P, C.c_uint32]),
+        "turner_set_guide_weighting": (C.c_int, [_P, C.c_int]),
         "turner_guide_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
         "turner_guide_destroy": (None, [_P]),
         "turner_guide_params": (C.c_int, [_P, _P, C.c_int]),
@@ -546,6 +547,10 @@ class Context:
         _check(_lib().turner_render_accumulate(self._h, C.byref(job), passes, _ptr(out), C.byref(total),
                                                HOST_BUFFERS), "turner_render_accumulate")
         return out, total.value
+
+    def set_guide_weighting(self, mode: int) -> None:
+        """Training-record weights: 0 incident radiance, 1 also by path throughput, 2 by its square root."""
+        _check(_lib().turner_set_guide_weighting(self._h, mode), "turner_set_guide_weighting")
 
     def set_guide_depth(self, depth: int) -> None:
         """Guided jobs sample from the proposal at hits of depth < depth."""

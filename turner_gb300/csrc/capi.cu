@@ -101,6 +101,7 @@ struct turner_ctx {
     uint32_t guide_records = 1u << 18;   // training samples per pass
     uint32_t guide_steps_per_pass = 16;   // Adam steps on each pass's samples
     int32_t guide_depth = 64;             // hits below this depth sample by cosine
+    int32_t guide_weighting = 0;          // training targets: 0 incident radiance, 1 / 2 also by path throughput
     DevBuf gfeat, gout, qa_rec, qb_rec, r_feat, r_dir, r_weight, r_path, r_lbefore, r_tafter, r_fcp, r_count;
     double guide_train_ms = 0.0;
     uint64_t graph_launches = 0;
@@ -866,7 +867,8 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             // skips itself when fewer than 128 bounces were recorded)
             KernelTimer kt(ctx, TURNER_KERNEL_GUIDE_TRAIN, true);
             int gs = guide::finalize_records(recs.count, recs.cap, ctx->L.as<float4>(), recs.path, recs.l_before,
-                                             recs.t_after, recs.fcos_pdf, recs.weight, ctx->stream);
+                                             recs.t_after, recs.fcos_pdf, recs.weight, ctx->guide_weighting,
+                                             ctx->stream);
             if (gs != TURNER_OK) return gs;
             for (uint32_t k = 0; k < ctx->guide_steps_per_pass; ++k) {
                 gs = guide::train_device(ctx->guide, recs.feat, recs.dir, recs.weight, recs.cap, recs.count, 128,
@@ -1256,6 +1258,12 @@ int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, 
     ctx->guide_train = train != 0 && guide;
     ctx->guide_lr = lr;
     if (records_per_pass) ctx->guide_records = records_per_pass;
+    return TURNER_OK;
+}
+
+int turner_set_guide_weighting(turner_ctx* ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 2) return TURNER_ERR_INVALID_ARG;
+    ctx->guide_weighting = mode;
     return TURNER_OK;
 }
 

@@ -760,25 +760,35 @@ int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uin
 // sampled direction is what the rest of the path added after the bounce,
 // divided by the throughput after it: L_in = (L_end - L_before) / T_after;
 // weight = L_in * f cos / p (the integrand over the sampling pdf, luminance).
+// mode 1 also weighs each record by the path throughput that reached the
+// bounce (luminance, t_after / fcos_pdf), so that the shared network spends
+// its capacity where the pixels' variance comes from: the weight becomes the
+// luminance the path gained after the bounce. Mode 2 weighs by the square
+// root of that throughput.
 __global__ void k_finalize_records(const uint32_t* __restrict__ count, uint32_t cap, const float4* __restrict__ L,
                                    const uint32_t* __restrict__ path, const float* __restrict__ l_before,
                                    const float* __restrict__ t_after, const float* __restrict__ fcos_pdf,
-                                   float* __restrict__ weight) {
+                                   float* __restrict__ weight, int mode) {
     const uint32_t n = min(*count, cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 l = L[path[i]];
         const float lum = 0.2126f * l.x + 0.7152f * l.y + 0.0722f * l.z;
         const float t = t_after[i];
-        const float lin = t > 0.f ? fmaxf(lum - l_before[i], 0.f) / t : 0.f;
-        weight[i] = fminf(lin * fcos_pdf[i], 1e4f);
+        const float fc = fcos_pdf[i];
+        const float gained = fmaxf(lum - l_before[i], 0.f);
+        const float lin = t > 0.f ? gained / t : 0.f;
+        float w = lin * fc;
+        if (mode == 1) w = gained;
+        else if (mode == 2) w = fc > 0.f ? w * sqrtf(t / fc) : 0.f;
+        weight[i] = fminf(w, 1e4f);
     }
 }
 
 int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const uint32_t* path,
-                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight,
+                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight, int mode,
                      cudaStream_t stream) {
     k_finalize_records<<<(cap + 255) / 256, 256, 0, stream>>>(count, cap, L, path, l_before, t_after, fcos_pdf,
-                                                              weight);
+                                                              weight, mode);
     return cuda_status(cudaGetLastError());
 }
 

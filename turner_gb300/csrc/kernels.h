@@ -170,7 +170,7 @@ namespace guide {
 int forward_queue(turner_guide* g, const float* feat, const uint32_t* n_dev, uint32_t cap, float* out,
                   cudaStream_t stream);
 int finalize_records(const uint32_t* count, uint32_t cap, const float4* L, const uint32_t* path,
-                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight,
+                     const float* l_before, const float* t_after, const float* fcos_pdf, float* weight, int mode,
                      cudaStream_t stream);
 // One Adam step on n samples, or on min(n, *n_dev) when n_dev is given; a
 // step with fewer than min_n samples changes nothing. Asynchronous unless
