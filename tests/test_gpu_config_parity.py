@@ -207,3 +207,37 @@ def test_shadow_decisions_per_ray(ctx, sphere_room_327k):
     # the same rays through the closest-hit entry point: the decision is that of its answer
     gid, gr, _, _ = ctx.intersect(sid, p2, ld)
     assert np.array_equal(gid, rid) and np.array_equal(gr.view(np.uint32), rr.view(np.uint32))
+
+
+@pytest.mark.parametrize("sampling", [tg.SAMPLING_UNIFORM, tg.SAMPLING_COSINE])
+def test_baffle_sphere_view_band_depth5(ctx, sampling):
+    """The 16-view workload's scene (the 327,680-triangle displaced sphere in
+    the baffled room, 368,654 triangles) seen from the circle view that looks
+    through the room's open front, 1920x1080 at depth 5: rows 536-544, 4
+    pixel samples."""
+    m = tg.make_scene(tg.SCENE_BAFFLE_SPHERE, detail=7, count=64, aspect=16 / 9)
+    nodes, tris, box = tg.KDTree.from_mesh(m).export()
+    sid = ctx.upload(nodes, tris, box)
+    sc = orc.Scene(nodes, tris, box)
+    cam = tg.look_at_camera((2.78, 1.5, -3.5 + 4.0), (2.78, 1.65, -3.5), 16 / 9)
+    job = tg.make_job(sid, m, 1920, 1080, pixel_samples=4, max_depth=5, seed=17, sampling=sampling, rows=(536, 544))
+    job.camera = cam
+    (img,), (st,) = ctx.render([job])
+    ref, rst = sc.render(cam, m.light, 1920, 1080, 4, 5, seed=17, sampling=sampling, rows=(536, 544))
+    check_close(img, ref[536:544])
+    check_rays(st.rays, rst[0])
+
+
+def test_large_soup_band(ctx):
+    """A scene of the batched workload's kind at its larger end: a clustered
+    soup of 100,000 triangles in the room, 1024 wide, 16 pixel samples,
+    depth 4, a 12-row band."""
+    m = tg.make_scene(tg.SCENE_SOUP, count=100_000, seed=1234)
+    nodes, tris, box = tg.KDTree.from_mesh(m).export()
+    sid = ctx.upload(nodes, tris, box)
+    sc = orc.Scene(nodes, tris, box)
+    job = tg.make_job(sid, m, 1024, 1024, pixel_samples=16, max_depth=4, seed=9, rows=(500, 512))
+    (img,), (st,) = ctx.render([job])
+    ref, rst = oracle_render(sc, m, job, rows=(500, 512))
+    check_close(img, ref[500:512])
+    check_rays(st.rays, rst[0])
