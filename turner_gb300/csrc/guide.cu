@@ -287,8 +287,9 @@ struct BwdSmem {
     uint8_t dy_km[128 * kHidden * 2];      // dY, K-major 128 x 48 / 64 (A of dX)
     uint8_t dyT[128 * 128 * 2];            // dY^T, K-major 128 x 128 samples, rows 64.. zero (A of dW)
     uint8_t xT[96 * 128 * 2];              // [X, 1]^T, K-major 80 / 96 x 128 samples (B of dW)
-    __nv_bfloat16 xrow[128 * kXRow];       // X_l, row per sample
+    __nv_bfloat16 xrow[2][128 * kXRow];    // X_l, row per sample; the other buffer receives the next X
     __nv_bfloat16 dyrow[128 * kDyRow];     // dY_l, row per sample
+    float head_out[128 * kOut];            // the tile's network outputs (arrive with the tile's X_4)
     uint64_t mbar;
     uint32_t tmem;
     int abort;
@@ -367,31 +368,50 @@ __device__ __forceinline__ uint4 gather8(const __nv_bfloat16* p, int stride) {
     return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// X_l of the tile's 128 samples from the forward's activations (336 BF16 per
-// sample: X_0 80, X_1..X_4 64 each), row-major into xrow; zeros past n.
-__device__ __forceinline__ void stage_x(BwdSmem& sm, const __nv_bfloat16* __restrict__ acts, uint32_t n, uint32_t s0,
-                                        int l, int t, int nt) {
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* src, bool valid) {
+    // src-size 0 fills the 16 bytes with zeros and reads nothing
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(tc::smem_u32(smem_dst)), "l"(src),
+                 "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Starts copying X_l of the tile at s0 (336 BF16 activations per sample: X_0
+// 80, X_1..X_4 64 each) row-major into `dst`, zeros past n; with the head
+// layer's X also the tile's 40 network outputs into head_out. Asynchronous
+// (cp.async): the copies land while the current layer computes; every thread
+// waits for its own copies (cp_async_wait_all) before the barrier that
+// precedes their use.
+__device__ __forceinline__ void stage_x_async(BwdSmem& sm, __nv_bfloat16* dst, const __nv_bfloat16* __restrict__ acts,
+                                              const float* __restrict__ out, uint32_t n, uint32_t s0, int l) {
     const int chunks = layer_in(l) / 8;
     const int off = l == 0 ? 0 : 80 + 64 * (l - 1);
-    for (int i = t; i < 128 * chunks; i += nt) {
+    for (int i = threadIdx.x; i < 128 * chunks; i += kBwdThreads) {
         const int r = i / chunks, c = i - r * chunks;
         const uint32_t s = s0 + static_cast<uint32_t>(r);
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (s < n) v = *reinterpret_cast<const uint4*>(acts + size_t(s) * 336 + off + 8 * c);
-        *reinterpret_cast<uint4*>(sm.xrow + r * kXRow + 8 * c) = v;
+        cp_async16(dst + r * kXRow + 8 * c, s < n ? acts + size_t(s) * 336 + off + 8 * c : acts, s < n);
     }
+    if (l == kLayers - 1) {
+        for (int i = threadIdx.x; i < 128 * (kOut / 4); i += kBwdThreads) {
+            const int r = i / (kOut / 4), c = i - r * (kOut / 4);
+            const uint32_t s = s0 + static_cast<uint32_t>(r);
+            cp_async16(sm.head_out + r * kOut + 4 * c, s < n ? out + size_t(s) * kOut + 4 * c : out, s < n);
+        }
+    }
+    cp_async_commit();
 }
 
 // [X_l, 1]^T (rows: the layer's inputs, then a ones row, then zero rows up to
 // dw_n(l)) and dY^T (rows: output units below n_pad, zeros up to 64), both
 // K-major over the 128 samples, from the staging buffers.
-__device__ __forceinline__ void build_transposes(BwdSmem& sm, int l) {
+__device__ __forceinline__ void build_transposes(BwdSmem& sm, const __nv_bfloat16* xrow, int l) {
     const int K = layer_in(l), N = dw_n(l), npad = layer_out_pad(l);
     const uint32_t one2 = 0x3F803F80u;   // two BF16 ones
     for (int c = threadIdx.x; c < N * 16; c += kBwdThreads) {
         const int k = c % N, j = c / N;
         uint4 u = make_uint4(0u, 0u, 0u, 0u);
-        if (k < K) u = gather8(sm.xrow + (8 * j) * kXRow + k, kXRow);
+        if (k < K) u = gather8(xrow + (8 * j) * kXRow + k, kXRow);
         else if (k == K) u = make_uint4(one2, one2, one2, one2);
         *reinterpret_cast<uint4*>(sm.xT + tc::kmajor_offset(static_cast<uint32_t>(k), 8u * j, 128)) = u;
     }
@@ -455,17 +475,21 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     float my_loss = 0.f;
     bool had_tile = false;
 
+    int cur = 0;   // xrow buffer holding the current X
+    if (blockIdx.x < tiles) stage_x_async(sm, sm.xrow[0], acts, out, n, blockIdx.x * 128, kLayers - 1);
     for (uint32_t tile = blockIdx.x; tile < tiles && !sm.abort; tile += gridDim.x) {
         const bool first = !had_tile;
         had_tile = true;
         const uint32_t s0 = tile * 128;
+        cp_async_wait_all();   // this tile's X_4 and network outputs
+        __syncthreads();
         if (tid < 128) {
             // head: dY of the output layer, 40 columns padded to 48
             const uint32_t s = s0 + static_cast<uint32_t>(tid);
             float g[kOut];
             if (s < n) {
                 float raw[kOut];
-                const float4* o4 = reinterpret_cast<const float4*>(out + size_t(s) * kOut);
+                const float4* o4 = reinterpret_cast<const float4*>(sm.head_out + tid * kOut);
 #pragma unroll
                 for (int q = 0; q < kOut / 4; ++q) {
                     const float4 v = o4[q];
@@ -490,13 +514,11 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
                 *reinterpret_cast<uint4*>(sm.dyrow + tid * kDyRow + 8 * q) = u;
                 *reinterpret_cast<uint4*>(sm.dy_km + tc::kmajor_offset(static_cast<uint32_t>(tid), 8u * q, kOutPad)) = u;
             }
-        } else {
-            stage_x(sm, acts, n, s0, kLayers - 1, tid - 128, 128);
         }
         for (int l = kLayers - 1; l >= 0; --l) {
-            // xrow = X_l, dyrow / dy_km = dY_l
+            // xrow[cur] = X_l, dyrow / dy_km = dY_l
             __syncthreads();
-            build_transposes(sm, l);
+            build_transposes(sm, sm.xrow[cur], l);
             tc::fence_async_smem();
             tc::tc_fence_before_sync();
             __syncthreads();
@@ -507,6 +529,13 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
                 issue_steps(tmem + static_cast<uint32_t>(dw_col(l)), sm.dyT, sm.xT, 128, dw_n(l), !first);
                 tc::mma_commit(&sm.mbar);
             }
+            // the next X into the other buffer while the products run: this
+            // tile's X_{l-1}, or after the first layer the next tile's X_4
+            // and network outputs (the other buffer's last reader finished
+            // before the barrier above)
+            if (l > 0) stage_x_async(sm, sm.xrow[cur ^ 1], acts, out, n, s0, l - 1);
+            else if (tile + gridDim.x < tiles) stage_x_async(sm, sm.xrow[cur ^ 1], acts, out, n,
+                                                             (tile + gridDim.x) * 128, kLayers - 1);
             if (!tc::mbar_wait(&sm.mbar, phase, err)) sm.abort = 1;
             phase ^= 1;
             tc::tc_fence_after_sync();
@@ -517,12 +546,13 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
             {
                 const int r = static_cast<int>(quad) * 32 + lane;
                 const uint32_t c0 = colh * 32u;
+                const __nv_bfloat16* xr = sm.xrow[cur];
                 float v[32];
                 tc::tmem_ld16(tmem + lane_base + c0, v);
                 tc::tmem_ld16(tmem + lane_base + c0 + 16u, v + 16);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const uint4 xv = *reinterpret_cast<const uint4*>(sm.xrow + r * kXRow + c0 + 8 * q);
+                    const uint4 xv = *reinterpret_cast<const uint4*>(xr + r * kXRow + c0 + 8 * q);
                     const uint32_t xw[4] = {xv.x, xv.y, xv.z, xv.w};
                     float y[8];
 #pragma unroll
@@ -537,10 +567,12 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
                                                                            kHidden)) = u;
                 }
             }
-            __syncthreads();   // X_l is no longer read
-            stage_x(sm, acts, n, s0, l - 1, tid, kBwdThreads);
+            cp_async_wait_all();   // X_{l-1} has landed (the barrier at the top of the loop publishes it)
+            cur ^= 1;
         }
+        cur ^= 1;   // the next tile's X_4 went to the other buffer
     }
+    cp_async_wait_all();   // no copy may outlive the kernel (an abort can leave one in flight)
     // loss, and this CTA's dW' out of TMEM into the global gradient
     for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_xor_sync(0xFFFFFFFFu, my_loss, off);
     if (lane == 0) atomicAdd(&sm.loss, my_loss);
