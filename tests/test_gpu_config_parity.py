@@ -91,7 +91,7 @@ def test_baffle_room_40k_band_depth5(ctx, sampling):
     """The indirect-lit room at its configured tessellation (64 x 64 quads per
     wall, 40,962 triangles) and depth 5: a 16-row band through the middle of
     the 1024x1024 frame, 8 pixel samples, uniform (the reference's) and cosine
-    (the plain tracer the learned proposal is judged against) sampling."""
+    (the plain tracer the learned proposal is compared with) sampling."""
     m = tg.make_scene(tg.SCENE_BAFFLE_ROOM, detail=64)
     assert m.n_triangles > 40000
     nodes, tris, box = tg.KDTree.from_mesh(m).export()
