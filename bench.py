@@ -619,6 +619,7 @@ def main() -> None:
     ap.add_argument("--traversal", default="parity", choices=["parity", "fast"])
     ap.add_argument("--chunk-paths", type=int, default=1 << 24)
     ap.add_argument("--speculative", action="store_true", help="speculative traversal rounds")
+    ap.add_argument("--no-packet", action="store_true", help="camera-ray warps traverse lane by lane, not as packets")
     ap.add_argument("--ring", type=int, default=0, choices=[0, 4, 8],
                     help="traversal stack entries kept in shared memory (0: all in local memory)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
@@ -690,6 +691,7 @@ def main() -> None:
     ctx.set_chunk_paths(args.chunk_paths)
     ctx.set_traversal_ring(args.ring)
     ctx.set_traversal_speculative(args.speculative)
+    ctx.set_traversal_packet(0 if args.no_packet else tg.PACKET_CAMERA)
     sid = ctx.upload_tree(tree)
     nodes, tris, box = tree.export()
     traversal = tg.TRAVERSAL_FAST if args.traversal == "fast" else tg.TRAVERSAL_PARITY
@@ -826,7 +828,7 @@ def main() -> None:
             "config": {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "nodes": int(nodes.size),
                        "width": WIDTH, "height": HEIGHT, "pixel_samples": SPP, "max_depth": DEPTH,
                        "monte_carlo_samples": MC, "traversal": args.traversal, "chunk_paths": args.chunk_paths,
-                       "stack_ring": args.ring, "speculative": args.speculative,
+                       "stack_ring": args.ring, "speculative": args.speculative, "camera_ray_packets": not args.no_packet,
                        "l2": "flushed between steps (512 MiB write outside the timed kernels)",
                        "parallelism": f"rows of one frame over {world} ranks" if world > 1 else "single GPU",
                        "kdtree_build_s": round(build_s, 3)},

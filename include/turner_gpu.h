@@ -240,6 +240,19 @@ int turner_set_traversal_ring(turner_ctx* ctx, uint32_t entries);
  * PARITY / shadow traversal (not FAST). Default off. No reference
  * counterpart: tuning knob of this library. */
 int turner_set_traversal_speculative(turner_ctx* ctx, int on);
+/* Packet traversal: a warp whose rays were all just taken, share their
+ * direction signs and their scene walks the tree as one: a cell is entered
+ * when some lane's interval overlaps it, each lane tests exactly the leaf
+ * runs its own traversal would, in the same order, and node words and
+ * triangle records are loaded once for the warp. Results do not change.
+ * mode is a mask: TURNER_PACKET_CAMERA (default) for the camera rays of
+ * renders (warps of neighbouring samples), TURNER_PACKET_BATCHED for every
+ * qualifying warp of turner_intersect, turner_occluded and
+ * turner_intersect_noalloc; 0 turns packets off. No reference counterpart:
+ * tuning knob of this library. */
+#define TURNER_PACKET_CAMERA 1
+#define TURNER_PACKET_BATCHED 2
+int turner_set_traversal_packet(turner_ctx* ctx, int mode);
 
 /* Per-kernel device time, measured with CUDA events on the context stream
  * around every launch while profiling is on. No reference counterpart: the

@@ -223,7 +223,7 @@ def test_full_hit_test_set(ctx, sphere_room_327k):
     assert np.array_equal(fast[0], cpu[0])
 
 
-@pytest.mark.parametrize("ring", [4, 8, "speculative"])
+@pytest.mark.parametrize("ring", [4, 8, "speculative", "packet"])
 def test_shared_memory_stack_is_exact(ctx, uploaded, ring):
     """The traversal stack with its newest 4 or 8 entries in shared memory
     and older ones in local memory, and speculative traversal rounds:
@@ -232,6 +232,8 @@ def test_shared_memory_stack_is_exact(ctx, uploaded, ring):
     def setting(on):
         if ring == "speculative":
             ctx.set_traversal_speculative(on)
+        elif ring == "packet":
+            ctx.set_traversal_packet(tg.PACKET_CAMERA | (tg.PACKET_BATCHED if on else 0))
         else:
             ctx.set_traversal_ring(ring if on else 0)
 
@@ -252,3 +254,35 @@ def test_shared_memory_stack_is_exact(ctx, uploaded, ring):
         assert np.array_equal(occ, occ2)
     with pytest.raises(tg.TurnerError):
         ctx.set_traversal_ring(5)
+
+
+def test_packet_traversal_of_coherent_rays_is_exact(ctx, uploaded):
+    """Camera-like ray bundles (32 rays with nearly one direction from one
+    point, so whole warps share their direction signs) traverse as packets
+    and give the oracle's answers bit for bit, for closest-hit and shadow
+    traversal, also with some bundles mixing direction signs."""
+    rng = np.random.default_rng(41)
+    for name in ("sphere5", "baffle32", "room"):
+        sid, ref, box = uploaded[name]
+        lo, hi = box[:3], box[3:]
+        n_b = 4096
+        orig = (lo + (hi - lo) * rng.uniform(0.2, 0.8, (n_b, 3))).astype(np.float32)
+        axis = rng.normal(size=(n_b, 3))
+        axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+        spread = np.where(np.arange(n_b)[:, None] % 7 == 0, 0.5, 0.02)   # every 7th bundle mixes signs
+        d = axis[:, None, :] + spread[:, None, :] * rng.normal(size=(n_b, 32, 3))
+        o = np.repeat(orig[:, None, :], 32, axis=1)
+        o, d = o.reshape(-1, 3).T.astype(np.float32), d.reshape(-1, 3).T.astype(np.float32)
+        tm = rng.uniform(0, 6, o.shape[1]).astype(np.float32)
+        want = ref.intersect(o, d)
+        occ0 = ctx.occluded(sid, o, d, tm)
+        ctx.set_traversal_packet(tg.PACKET_CAMERA | tg.PACKET_BATCHED)
+        try:
+            got = ctx.intersect(sid, o, d)
+            occ1 = ctx.occluded(sid, o, d, tm)
+        finally:
+            ctx.set_traversal_packet(tg.PACKET_CAMERA)
+        assert_same(got, want)
+        assert np.array_equal(occ0, occ1)
+        rid, rr = want[0], want[1]
+        assert np.array_equal(occ1, (rid < tg.MISS) & ~(rr > tm))

@@ -141,6 +141,7 @@ def test_refill_thresholds_are_invisible(ctx):
                 ctx.set_traversal_refill(k, lanes)
             ctx.set_traversal_ring(8 if lanes == 7 else 0)
             ctx.set_traversal_speculative(lanes == 32)
+            ctx.set_traversal_packet(tg.PACKET_CAMERA if lanes != 32 else 0)
             (b,), (sb,) = ctx.render([job])
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and sa.rays == sb.rays
             h2 = ctx.intersect(sid, o, d)
@@ -150,6 +151,7 @@ def test_refill_thresholds_are_invisible(ctx):
     finally:
         ctx.set_traversal_ring(0)
         ctx.set_traversal_speculative(False)
+        ctx.set_traversal_packet(tg.PACKET_CAMERA)
         for k, v in zip(kinds, defaults):
             ctx.set_traversal_refill(k, v)
 

@@ -52,6 +52,7 @@ TRIANGLE_FLOATS = 48  # turner_triangle: Triangle::serialize order
 
 GRAPH_AUTO, GRAPH_ALWAYS, GRAPH_NEVER = 0, 1, 2
 RAYS_PRIMARY, RAYS_BOUNCE, RAYS_SHADOW_PRIMARY, RAYS_SHADOW, RAYS_INTERSECT = 0, 1, 2, 3, 4
+PACKET_CAMERA, PACKET_BATCHED = 1, 2
 RENDERER_PATH, RENDERER_RAYTRACE, RENDERER_RAYCAST = 0, 1, 2
 KERNEL_NAMES = ("k_camera", "k_trace", "k_shade", "k_shadow", "k_resolve", "k_intersect", "k_guide_features",
                 "k_mlp_forward", "guide_train")
@@ -133,6 +134,7 @@ def _lib() -> C.CDLL:
         "turner_set_traversal_refill": (C.c_int, [_P, C.c_int, C.c_uint32]),
         "turner_set_traversal_ring": (C.c_int, [_P, C.c_uint32]),
         "turner_set_traversal_speculative": (C.c_int, [_P, C.c_int]),
+        "turner_set_traversal_packet": (C.c_int, [_P, C.c_int]),
         "turner_kernel_times": (C.c_int, [_P, _P, _P, C.c_int]),
         "turner_upload_scene": (C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, _P, C.POINTER(C.c_uint32)]),
         "turner_free_scene": (C.c_int, [_P, C.c_uint32]),
@@ -431,6 +433,12 @@ class Context:
         """A warp of the persistent traversal takes new rays of this kind
         (RAYS_*) only once `lanes` of its lanes are idle."""
         _check(_lib().turner_set_traversal_refill(self._h, kind, lanes), "turner_set_traversal_refill")
+
+    def set_traversal_packet(self, mode: int) -> None:
+        """Where warps of fresh rays with one direction octant traverse as
+        packets (same results): a mask of PACKET_CAMERA (renders' camera
+        rays, the default) and PACKET_BATCHED (intersect / occluded)."""
+        _check(_lib().turner_set_traversal_packet(self._h, int(mode)), "turner_set_traversal_packet")
 
     def set_traversal_speculative(self, on: bool) -> None:
         """Speculative traversal rounds (same results)."""

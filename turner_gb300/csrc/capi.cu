@@ -112,6 +112,7 @@ struct turner_ctx {
     // hit 173.7 -> 143.1 ms, their shadow rays 74.8 -> 60.0 ms in total);
     // incoherent bounce and shadow rays want nearly every idle lane refilled
     uint32_t refill[TURNER_RAYS_KINDS] = {32, 2, 32, 4, 1};
+    int packet_mode = TURNER_PACKET_CAMERA;   // where warps of coherent fresh rays traverse as packets
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t chunk_paths = 1u << 24;   // paths in flight per render pass
     uint64_t launches = 0;
@@ -487,6 +488,7 @@ int turner_intersect(turner_ctx* ctx, uint32_t scene_id, const float* ox, const 
     if (sc.height > 64) cfg.stack = kStackCap;
     cfg.work = ctx->work.as<uint32_t>();
     cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
+    cfg.packet = (ctx->packet_mode & TURNER_PACKET_BATCHED) != 0;
     if (flags == TURNER_DEVICE_BUFFERS) {
         for (uint64_t b = 0; b < n; b += (1ull << 30)) {
             const uint64_t m = std::min<uint64_t>(n - b, 1ull << 30);
@@ -544,6 +546,7 @@ int turner_occluded(turner_ctx* ctx, uint32_t scene_id, const float* ox, const f
     TraverseCfg cfg = ctx->traverse;
     cfg.work = ctx->work.as<uint32_t>();
     cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
+    cfg.packet = (ctx->packet_mode & TURNER_PACKET_BATCHED) != 0;
     // slices of at most 2^30 rays (the work counter is 32 bits)
     const uint64_t slice = flags == TURNER_DEVICE_BUFFERS ? std::min<uint64_t>(n, 1ull << 30)
                                                           : std::min<uint64_t>(n, 1ull << 24);
@@ -628,6 +631,12 @@ int turner_probe_gather(turner_ctx* ctx, uint64_t buffer_bytes, uint32_t load_by
 int turner_set_chunk_paths(turner_ctx* ctx, uint32_t paths) {
     if (!ctx || paths < 1024) return TURNER_ERR_INVALID_ARG;
     ctx->chunk_paths = paths;
+    return TURNER_OK;
+}
+
+int turner_set_traversal_packet(turner_ctx* ctx, int mode) {
+    if (!ctx || mode < 0 || mode > (TURNER_PACKET_CAMERA | TURNER_PACKET_BATCHED)) return TURNER_ERR_INVALID_ARG;
+    ctx->packet_mode = mode;
     return TURNER_OK;
 }
 
@@ -822,6 +831,10 @@ int launch_batch(turner_ctx* ctx, const Batch& b, double4* acc) {
             shadow_cfg.work = cnt + 3 * (b.levels + 1) + depth;
             trace_cfg.refill = ctx->refill[depth == 0 ? TURNER_RAYS_PRIMARY : TURNER_RAYS_BOUNCE];
             shadow_cfg.refill = ctx->refill[depth == 0 ? TURNER_RAYS_SHADOW_PRIMARY : TURNER_RAYS_SHADOW];
+            // packets where whole warps of coherent rays arrive: camera rays (their
+            // shadow rays measured slower as packets)
+            trace_cfg.packet = (ctx->packet_mode & TURNER_PACKET_CAMERA) && depth == 0;
+            shadow_cfg.packet = false;
             {
                 KernelTimer kt(ctx, TURNER_KERNEL_TRACE);
                 launch_trace(single, jobs, cur, ctx->hits.as<Hit>(), c.n_rays, fast, trace_cfg, ctx->stream);
@@ -1378,6 +1391,7 @@ int turner_intersect_noalloc(turner_ctx* ctx, uint32_t scene_id, const float* ox
     TraverseCfg cfg = ctx->traverse;
     if (sc.height > 64) cfg.stack = kStackCap;
     cfg.refill = ctx->refill[TURNER_RAYS_INTERSECT];
+    cfg.packet = (ctx->packet_mode & TURNER_PACKET_BATCHED) != 0;
     cfg.work = scratch;
     {
         KernelTimer kt(ctx, TURNER_KERNEL_INTERSECT);

@@ -523,6 +523,98 @@ __device__ __forceinline__ bool trav_round_spec(TravState& s, bool live, float t
     return hit_any || s.node == kNoNode;
 }
 
+// Packet traversal of a warp whose live rays share their direction signs
+// (`neg`) and scene (`nodes`, `tri`): camera rays of neighbouring pixels and
+// their shadow rays. Called by all 32 lanes; it runs until every live ray is
+// finished. The warp walks the tree as one: a child is entered when some
+// lane's interval overlaps it, the near child first, so every lane visits the
+// cells its own traversal (trav_round) would visit, in the same order, with
+// the same [tenter, texit], and tests the same leaf runs with the same
+// bounds: the answers are bit-identical. Lanes whose interval misses a cell
+// only wait while the warp is inside it. Node words and triangle records are
+// then the same address in every lane, one load for the warp.
+// A stack entry holds the far child (with the lane's "continues there" bit)
+// and the lane's entry and exit distances for it.
+template <bool ANY>
+__device__ __forceinline__ void trav_packet(TravState& s, bool live, float tmax, uint32_t neg,
+                                            const uint2* __restrict__ nodes, const float4* __restrict__ tri) {
+    uint4 pk[kStackCap];
+    bool alive = live, done = false;
+    float tenter = s.tenter, texit = s.texit;
+    uint32_t node = 0;
+    int sp = 0;
+    for (;;) {
+        uint2 w = __ldg(nodes + node);
+        if ((w.x & 3u) != 3u) {
+            const uint32_t ax = w.x & 3u;
+            const float t = (__uint_as_float(w.y) - pick(s.o, ax)) * pick(s.inv, ax);
+            uint32_t near_c = node + 1, far_c = w.x >> 2;
+            if (neg & (1u << ax)) {
+                const uint32_t tmp = near_c;
+                near_c = far_c;
+                far_c = tmp;
+            }
+            // the cases of trav_round: near only, far only, or both (far pushed)
+            const bool both = alive && !(texit < t) && !(t < tenter);
+            const bool want_near = alive && (texit < t || both);
+            const bool want_far = alive && !(texit < t) && (t < tenter || both);
+            const bool any_near = __any_sync(0xFFFFFFFFu, want_near);
+            const bool any_far = __any_sync(0xFFFFFFFFu, want_far);
+            if (any_near || any_far) {
+                if (any_near && any_far) {
+                    pk[sp] = make_uint4(far_c | (want_far ? 0x80000000u : 0u), __float_as_uint(both ? t : tenter),
+                                        __float_as_uint(texit), 0u);
+                    ++sp;
+                }
+                if (any_near) {
+                    node = near_c;
+                    alive = want_near;
+                    if (both) texit = t;
+                } else {
+                    node = far_c;
+                    alive = want_far;
+                }
+                continue;
+            }
+        } else if (__any_sync(0xFFFFFFFFu, alive)) {
+            // the leaf run: the same words for every lane, tested by the lanes inside the cell
+            uint32_t wi = node;
+            for (;;) {
+                const bool pair = w.x != 0xFFFFFFFFu;
+                uint2 next = w;
+                if (pair) next = __ldg(nodes + wi + 1);
+                float r, u, v;
+                if (alive && triangle_test_bounded<ANY>(tri, w.y, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+                    s.best = Hit{w.y, r, u, v};
+                    if (ANY) {
+                        alive = false;
+                        done = true;
+                    }
+                }
+                if (!pair) break;
+                const uint32_t id2 = w.x >> 2;
+                if (alive && triangle_test_bounded<ANY>(tri, id2, s.o, s.d, ANY ? tmax : s.best.r, r, u, v)) {
+                    s.best = Hit{id2, r, u, v};
+                    if (ANY) {
+                        alive = false;
+                        done = true;
+                    }
+                }
+                ++wi;
+                w = next;
+                if ((w.x & 3u) != 3u) break;
+            }
+        }
+        if (sp == 0) break;
+        --sp;
+        const uint4 e = pk[sp];
+        node = e.x & 0x7FFFFFFFu;
+        alive = (e.x >> 31) != 0u && !done;
+        tenter = __uint_as_float(e.y);
+        texit = __uint_as_float(e.z);
+    }
+}
+
 // xorshift64* (lib/xorshift.h:27-70): float = (x & (2^24 - 1)) * 2^-24
 __device__ __forceinline__ float xorshift_float(uint64_t& s) {
     s ^= s >> 12;

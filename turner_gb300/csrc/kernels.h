@@ -104,6 +104,8 @@ struct TraverseCfg {
     unsigned min_blocks = 10;     // 10, 12, 16: cap registers so that many blocks fit per SM (128-thread
                                   // blocks); 0: no cap. 10 (48 registers) is fastest on GB300
     unsigned refill = 1;          // persistent: a warp takes new rays once this many lanes are idle (1..32)
+    bool packet = false;          // warps of fresh rays with one direction octant traverse as packets
+                                  // (128-thread blocks, 10 per SM, no mailbox, not FAST); results unchanged
     bool speculative = false;     // speculative traversal rounds (128-thread blocks, 10 per SM, no mailbox,
                                   // not FAST); results are unchanged
     unsigned ring = 0;            // 4 or 8: the stack's newest entries in shared memory (128-thread blocks,

@@ -674,7 +674,8 @@ struct OccSrc {             // turner_occluded batches: any hit with r <= tmax[i
 // neighbouring rays of a coherent queue (camera rays) stay together and share
 // node and record loads. MULTI: every ray names its job and is traced in
 // that job's scene.
-template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, bool SPEC = false, class Stack>
+template <class Src, bool ANY, bool FAST, bool MULTI, int STACK, bool MAILBOX, bool SPEC = false,
+          bool PACKET = false, class Stack>
 __device__ __forceinline__ void traverse_persistent(const SceneView& single, const JobDesc* __restrict__ jobs,
                                                     Src& src, uint32_t* __restrict__ work, uint32_t refill,
                                                     Stack& st) {
@@ -682,6 +683,7 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
     TravState s;
     uint32_t cur = 0;
     bool active = false, exhausted = false;
+    bool fresh = false;   // PACKET: the lane's ray has not been advanced yet
     float tmax = 0.f;
     for (;;) {
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
@@ -706,6 +708,7 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
                         if (in_box) {
                             cur = idx;
                             active = true;
+                            fresh = true;
                             st.reset();
                         } else {
                             src.store(idx, s.best);   // misses the scene box
@@ -714,7 +717,31 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
                 }
             }
         }
-        if (__ballot_sync(0xFFFFFFFFu, active) == 0) break;
+        const unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+        if (act == 0) break;
+        if constexpr (PACKET && !FAST) {
+            // a warp of fresh rays with the same direction signs and scene
+            // walks the tree as a packet (same answers as the lanes alone)
+            if (__ballot_sync(0xFFFFFFFFu, active && fresh) == act && __popc(act) >= 8) {
+                const int lead = __ffs(act) - 1;
+                const uint32_t neg0 = __shfl_sync(0xFFFFFFFFu, s.neg, lead);
+                const unsigned long long n0 =
+                    __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(s.nodes), lead);
+                const unsigned long long t0 =
+                    __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(s.tri), lead);
+                const bool same = !active || (s.neg == neg0 && reinterpret_cast<unsigned long long>(s.nodes) == n0);
+                if (__all_sync(0xFFFFFFFFu, same)) {
+                    trav_packet<ANY>(s, active, tmax, neg0, reinterpret_cast<const uint2*>(n0),
+                                     reinterpret_cast<const float4*>(t0));
+                    if (active) {
+                        src.store(cur, s.best);
+                        active = false;
+                    }
+                    continue;
+                }
+            }
+            fresh = false;
+        }
         if constexpr (SPEC) {
             // every lane takes part in the speculative round's warp votes
             const bool done = trav_round_spec<ANY, MAILBOX>(s, active, tmax, st);
@@ -735,11 +762,15 @@ __device__ __forceinline__ void traverse_persistent(const SceneView& single, con
 // the uncapped kernel gives only the block size.
 // RING > 0: the stack's newest RING entries in shared memory (RingStack,
 // 8 * RING bytes per thread of dynamic shared memory), else all in local memory.
-// RING == -1: the local-memory stack with speculative rounds (trav_round_spec).
+// RING == -1: the local-memory stack with speculative rounds (trav_round_spec);
+// RING == -2: the local-memory stack, warps of coherent fresh rays as packets (trav_packet).
 template <class Src, bool ANY, bool FAST, bool MULTI, int BLOCK, int STACK, bool MAILBOX, int RING>
 __device__ __forceinline__ void traverse_body(const SceneView& single, const JobDesc* __restrict__ jobs, Src& src,
                                               uint32_t* __restrict__ work, uint32_t refill) {
-    if constexpr (RING < 0) {
+    if constexpr (RING == -2) {
+        LocalStack<STACK> st;
+        traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX, false, true>(single, jobs, src, work, refill, st);
+    } else if constexpr (RING < 0) {
         LocalStack<STACK> st;
         traverse_persistent<Src, ANY, FAST, MULTI, STACK, MAILBOX, true>(single, jobs, src, work, refill, st);
     } else if constexpr (RING > 0) {
@@ -878,6 +909,12 @@ void run_traverse(const SceneView& single, const JobDesc* jobs, const Src& src, 
     case 12: TURNER_SHAPE(ST, MB, 12); break;             \
     case 16: TURNER_SHAPE(ST, MB, 16); break;             \
     default: TURNER_SHAPE(ST, MB, 1); break;              \
+    }
+    if (cfg.packet && !FAST && !cfg.mailbox && cfg.min_blocks == 10 && !cfg.speculative && !cfg.ring) {
+        // warps of coherent fresh rays traverse as packets
+        run_traverse_shape<Src, ANY, FAST, MULTI, 128, kStackCap, false, 10, -2>(single, jobs, src, capacity, cfg,
+                                                                                 stream);
+        return;
     }
     if (cfg.speculative && !FAST && !cfg.mailbox && cfg.min_blocks == 10) {
         // speculative rounds (not with FAST's early stop)
