@@ -358,7 +358,10 @@ int turner_render(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, floa
  *                  blocks fit per SM (48, 40, 32 registers), 0: no cap.
  *                  Default 10: the traversal is latency-bound and 10 blocks
  *                  beat the uncapped 9 (56 registers) and the 12 at 40
- *                  registers, which spill more */
+ *                  registers, which spill more
+ *   refill_camera, refill_bounce, packets: the warp refill thresholds of
+ *                  camera and bounce rays and camera-ray packets (see
+ *                  turner_set_traversal_refill / _packet) */
 typedef struct turner_tuning {
     int32_t persistent;
     uint32_t blocks_per_sm;
@@ -369,6 +372,9 @@ typedef struct turner_tuning {
     uint32_t min_blocks;
     double ms;             /* device time of the batch with this configuration */
     uint32_t candidates;   /* configurations timed (0: taken from the cache)  */
+    uint32_t refill_camera;   /* turner_set_traversal_refill for camera rays (1..32) */
+    uint32_t refill_bounce;   /* and for bounce rays (1..32)                         */
+    uint32_t packets;         /* 1: camera-ray warps as packets (turner_set_traversal_packet) */
 } turner_tuning;
 /* Times configurations on the given batch (coordinate descent over the
  * fields above, two renders each, CUDA events) and applies the fastest to the

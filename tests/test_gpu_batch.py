@@ -164,16 +164,24 @@ def test_autotune_caches_and_keeps_images(ctx, scenes, tmp_path, monkeypatch):
     after, _ = ctx.render(jobs)
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
-    for shape in ({"block": 256, "stack": 64, "mailbox": 0, "min_blocks": 0},
-                  {"block": 128, "stack": 128, "mailbox": 1, "min_blocks": 12},
-                  {"block": 128, "stack": 64, "mailbox": 1, "min_blocks": 0}):
+    assert 1 <= t.refill_camera <= 32 and 1 <= t.refill_bounce <= 32 and t.packets in (0, 1)
+    for shape in ({"block": 256, "stack": 64, "mailbox": 0, "min_blocks": 0, "refill_camera": 16, "packets": 0},
+                  {"block": 128, "stack": 128, "mailbox": 1, "min_blocks": 12, "refill_bounce": 4},
+                  {"block": 128, "stack": 64, "mailbox": 1, "min_blocks": 0, "refill_camera": 8,
+                   "refill_bounce": 1}):
         tt = ctx.get_tuning()
-        tt.block, tt.stack, tt.mailbox, tt.min_blocks = shape["block"], shape["stack"], shape["mailbox"], \
-            shape["min_blocks"]
+        for k, v in shape.items():
+            setattr(tt, k, v)
         ctx.set_tuning(tt)
         again, _ = ctx.render(jobs)
         for a, b in zip(before, again):
             assert np.array_equal(a, b)
+    for field, bad in (("refill_camera", 0), ("refill_bounce", 33), ("packets", 2)):
+        tt = ctx.get_tuning()
+        setattr(tt, field, bad)
+        with pytest.raises(tg.TurnerError) as e:
+            ctx.set_tuning(tt)
+        assert e.value.status == tg.ERR_INVALID_ARG
     ctx.set_tuning(default)
 
 

@@ -95,7 +95,7 @@ def test_tuned_shapes_agree(ctx, uploaded, block, stack, mailbox, min_blocks):
     for name in ("sphere5", "soup20k"):
         sid, ref, box = uploaded[name]
         o, d = tg.make_rays(150_000, box, seed=41)
-        ctx.set_tuning(tg.Tuning(1, 0, block, stack, 1 << 24, mailbox, min_blocks, 0.0, 0))
+        ctx.set_tuning(tg.Tuning(1, 0, block, stack, 1 << 24, mailbox, min_blocks, 0.0, 0, 32, 2, 1))
         try:
             gpu = ctx.intersect(sid, o, d)
             fast = ctx.intersect(sid, o, d, mode=tg.TRAVERSAL_FAST)

@@ -93,7 +93,8 @@ class Job(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("persistent", C.c_int32), ("blocks_per_sm", C.c_uint32), ("block", C.c_uint32),
                 ("stack", C.c_uint32), ("chunk_paths", C.c_uint32), ("mailbox", C.c_uint32),
-                ("min_blocks", C.c_uint32), ("ms", C.c_double), ("candidates", C.c_uint32)]
+                ("min_blocks", C.c_uint32), ("ms", C.c_double), ("candidates", C.c_uint32),
+                ("refill_camera", C.c_uint32), ("refill_bounce", C.c_uint32), ("packets", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -1104,8 +1104,9 @@ bool tuning_lookup(const std::string& key, turner_tuning& t) {
     while (std::fgets(line, sizeof(line), f)) {
         char k[256];
         turner_tuning r{};
-        if (std::sscanf(line, "%255s %d %u %u %u %u %u %u %lf", k, &r.persistent, &r.blocks_per_sm, &r.block,
-                        &r.stack, &r.chunk_paths, &r.mailbox, &r.min_blocks, &r.ms) == 9 && key == k) {
+        if (std::sscanf(line, "%255s %d %u %u %u %u %u %u %lf %u %u %u", k, &r.persistent, &r.blocks_per_sm, &r.block,
+                        &r.stack, &r.chunk_paths, &r.mailbox, &r.min_blocks, &r.ms, &r.refill_camera,
+                        &r.refill_bounce, &r.packets) == 12 && key == k) {
             t = r;
             found = true;   // the last entry for a key wins
         }
@@ -1117,8 +1118,8 @@ bool tuning_lookup(const std::string& key, turner_tuning& t) {
 void tuning_store(const std::string& key, const turner_tuning& t) {
     FILE* f = std::fopen(tuning_cache_path().c_str(), "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %u %u %u %u %u %u %.4f\n", key.c_str(), t.persistent, t.blocks_per_sm, t.block, t.stack,
-                 t.chunk_paths, t.mailbox, t.min_blocks, t.ms);
+    std::fprintf(f, "%s %d %u %u %u %u %u %u %.4f %u %u %u\n", key.c_str(), t.persistent, t.blocks_per_sm, t.block,
+                 t.stack, t.chunk_paths, t.mailbox, t.min_blocks, t.ms, t.refill_camera, t.refill_bounce, t.packets);
     std::fclose(f);
 }
 
@@ -1132,6 +1133,9 @@ void apply_tuning(turner_ctx* ctx, const turner_tuning& t) {
     ctx->traverse.mailbox = t.mailbox != 0;
     ctx->traverse.min_blocks = valid_min_blocks(t.min_blocks) ? t.min_blocks : 0;
     ctx->chunk_paths = std::max<uint32_t>(1024, t.chunk_paths);
+    if (t.refill_camera >= 1 && t.refill_camera <= 32) ctx->refill[TURNER_RAYS_PRIMARY] = t.refill_camera;
+    if (t.refill_bounce >= 1 && t.refill_bounce <= 32) ctx->refill[TURNER_RAYS_BOUNCE] = t.refill_bounce;
+    ctx->packet_mode = (ctx->packet_mode & ~TURNER_PACKET_CAMERA) | (t.packets ? TURNER_PACKET_CAMERA : 0);
 }
 
 } // namespace
@@ -1141,7 +1145,8 @@ extern "C" {
 int turner_set_tuning(turner_ctx* ctx, const turner_tuning* t) {
     if (!ctx || !t) return TURNER_ERR_INVALID_ARG;
     if ((t->block != 128 && t->block != 256) || (t->stack != 64 && t->stack != kStackCap) || t->blocks_per_sm > 64 ||
-        t->chunk_paths < 1024 || t->mailbox > 1 || !valid_min_blocks(t->min_blocks))
+        t->chunk_paths < 1024 || t->mailbox > 1 || !valid_min_blocks(t->min_blocks) || t->refill_camera < 1 ||
+        t->refill_camera > 32 || t->refill_bounce < 1 || t->refill_bounce > 32 || t->packets > 1)
         return TURNER_ERR_INVALID_ARG;
     apply_tuning(ctx, *t);
     return TURNER_OK;
@@ -1158,6 +1163,9 @@ int turner_get_tuning(turner_ctx* ctx, turner_tuning* t) {
     t->min_blocks = ctx->traverse.min_blocks;
     t->ms = 0;
     t->candidates = 0;
+    t->refill_camera = ctx->refill[TURNER_RAYS_PRIMARY];
+    t->refill_bounce = ctx->refill[TURNER_RAYS_BOUNCE];
+    t->packets = (ctx->packet_mode & TURNER_PACKET_CAMERA) ? 1 : 0;
     return TURNER_OK;
 }
 
@@ -1205,7 +1213,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
         return TURNER_OK;
     };
     // coordinate descent from the defaults, one knob at a time
-    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 10, 0, 0};
+    turner_tuning cur{1, 0, 128, kStackCap, 1u << 24, 0, 10, 0, 0, 32, 2, 1};
     int s = measure(cur, cur.ms);
     if (s != TURNER_OK) return s;
     const uint32_t blocks[] = {128, 256};
@@ -1254,6 +1262,21 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
                 t.min_blocks = v;
                 return true;
             }, std::vector<uint32_t>{0, 12, 16});
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.refill_camera == v) return false;
+                t.refill_camera = v;
+                return true;
+            }, std::vector<uint32_t>{16, 8});
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) {
+                if (t.refill_bounce == v) return false;
+                t.refill_bounce = v;
+                return true;
+            }, std::vector<uint32_t>{1, 4});
+    if (s == TURNER_OK)
+        s = try_value([&](turner_tuning& t, uint32_t v) { if (t.packets == v) return false; t.packets = v; return true; },
+                      std::vector<uint32_t>{0});
     if (s == TURNER_OK)
         s = try_value([&](turner_tuning& t, int v) { if (t.persistent == v) return false; t.persistent = v; return true; },
                       std::vector<int>{0});
