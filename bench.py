@@ -47,6 +47,8 @@ WORKLOAD = "sphere_room_327k_1920x1080_16spp_d3"
 METRIC = "Mrays/s (reference ray count: primary + bounce rays incl. misses, excl. shadow rays)"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC = ROOT / "profiles" / "k_trace_traffic.json"
+# training objectives of the learned proposal (turner_guide_set_objective)
+OBJECTIVES = {"kl": 0, "variance": 1}
 
 
 def rank_info():
@@ -408,10 +410,16 @@ def run_guide(args) -> None:
                           steps_per_pass=args.guide_steps)
         training = guide is not None
         t = time.perf_counter()
+        train_s = args.train_fraction * args.budget
         while True:
-            if training and time.perf_counter() - t > args.train_fraction * args.budget:
+            if training and time.perf_counter() - t > train_s:
                 ctx.set_guide(guide, train=False)   # the rest of the budget renders with the trained network
                 training = False
+            elif training and args.guide_lr_end > 0:
+                # exponential learning-rate decay over the training window
+                frac = min(1.0, (time.perf_counter() - t) / train_s)
+                ctx.set_guide(guide, train=True, lr=args.guide_lr * (args.guide_lr_end / args.guide_lr) ** frac,
+                              records=args.guide_records, steps_per_pass=args.guide_steps)
             ctx.accumulate(job(sampling, args.pass_spp, seed + 1), 1, readback=False)
             if time.perf_counter() - t >= args.budget:
                 break
@@ -425,6 +433,7 @@ def run_guide(args) -> None:
             seed = 7 + 1000 * rep
             plain, plain_spp, plain_s = run(tg.SAMPLING_COSINE, seed)
             guide = tg.Guide(ctx, seed=11 + rep)
+            guide.set_objective(OBJECTIVES[args.guide_objective])
             learned, learned_spp, learned_s = run(tg.SAMPLING_GUIDED, seed, guide)
             steps, loss, train_ms = ctx.guide_stats()
             ctx.set_guide(None)
@@ -449,7 +458,8 @@ def run_guide(args) -> None:
                    "pass_spp": args.pass_spp, "train_fraction": args.train_fraction,
                    "records_per_pass": args.guide_records, "steps_per_pass": args.guide_steps,
                    "lr": args.guide_lr, "repeats": args.guide_repeats, "guide_depth": args.guide_depth,
-                   "guide_weighting": args.guide_weighting},
+                   "guide_weighting": args.guide_weighting, "guide_objective": args.guide_objective,
+                   "lr_end": args.guide_lr_end},
         "repeats": reps,
         "clocks": clk.summary,
     }))
@@ -495,6 +505,7 @@ def run_views16(args) -> None:
     outs = [torch.empty((H, W, 4), dtype=torch.float32, device="cuda") for _ in cams]
     ptrs = [o.data_ptr() for o in outs]
     guide = tg.Guide(ctx, seed=11)
+    guide.set_objective(OBJECTIVES[args.guide_objective])
     ctx.set_guide(guide, train=True, lr=args.guide_lr, records=args.guide_records, steps_per_pass=args.guide_steps)
     t = time.perf_counter()
     calls = 0
@@ -570,6 +581,7 @@ def run_views16(args) -> None:
             seed = 7 + 1000 * rep
             plain, plain_spp, plain_s = accumulate(tg.SAMPLING_COSINE, args.pass_spp, seed, budget=args.budget)
             g2 = tg.Guide(ctx, seed=12 + rep)
+            g2.set_objective(OBJECTIVES[args.guide_objective])
             ctx.set_guide(g2, train=False)
             ctx.render(band_jobs(args.pass_spp, tg.SAMPLING_GUIDED, 3), sptr, tg.DEVICE_BUFFERS)   # workspace
             ctx.set_guide(g2, train=True, lr=args.guide_lr, records=args.guide_records,
@@ -591,7 +603,7 @@ def run_views16(args) -> None:
         "dtype": "bf16 MLP / f32 tracing", "data": "synthetic",
         "config": {"workload": f"baffled room + displaced icosphere, 16 views 1920x1080 x {args.views_spp} spp, depth 5",
                    "triangles": int(mesh.n_triangles), "views_radius": args.views_radius,
-                   "host_tree_build_s": round(build_s, 2)},
+                   "host_tree_build_s": round(build_s, 2), "guide_objective": args.guide_objective},
         "guided": thr["guided"], "cosine": thr["cosine"],
         "training": {"calls": calls, "wall_s": round(train_wall, 2), "adam_steps": int(steps),
                      "last_loss": round(loss, 4), "train_ms": round(train_ms, 1)},
@@ -644,8 +656,12 @@ def main() -> None:
     ap.add_argument("--guide-records", type=int, default=1 << 18)
     ap.add_argument("--guide-lr", type=float, default=1e-3)
     ap.add_argument("--guide-steps", type=int, default=16, help="Adam steps per training pass")
+    ap.add_argument("--guide-lr-end", type=float, default=0.0,
+                    help="guide: decay the learning rate exponentially to this value over the training window (0: constant)")
     ap.add_argument("--guide-repeats", type=int, default=3, help="guide: independent seeds (fresh networks)")
     ap.add_argument("--guide-depth", type=int, default=64, help="guided sampling at hits of depth < this")
+    ap.add_argument("--guide-objective", default="kl", choices=sorted(OBJECTIVES),
+                    help="training objective of the proposal: KL divergence or the 50/50 estimator's variance")
     ap.add_argument("--guide-weighting", type=int, default=0, choices=[0, 1, 2],
                     help="training-record weights: 0 incident radiance, 1 x path throughput, 2 x its square root")
     ap.add_argument("--batch-scenes", type=int, default=64)

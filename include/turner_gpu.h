@@ -415,11 +415,16 @@ int turner_render_accumulate(turner_ctx* ctx, const turner_job* job, uint32_t pa
  *   features  9 floats per sample: position in [0,1]^3 (scene box), shading
  *             normal, albedo
  *   output    40 floats per sample: 8 x (direction, log concentration, logit)
- *   loss      mean over samples of -weight * log q(direction)
+ *   loss      mean over samples of -weight * log q(direction) (the KL
+ *             objective; turner_guide_set_objective below)
  * Parameters: TURNER_GUIDE_PARAMS floats, W1 b1 ... W5 b5 (W row-major
  * [out x in]; layers 80->64->64->64->64->40). */
 #define TURNER_GUIDE_PARAMS 20264
 typedef struct turner_guide turner_guide;
+/* A proposal runs on the stream of the context it was created on. Destroying
+ * it unbinds it from that context (turner_set_guide). Destroying the context
+ * first is allowed: the proposal then accepts turner_guide_destroy only, and
+ * its other calls return TURNER_ERR_INVALID_ARG. */
 int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out);
 void turner_guide_destroy(turner_guide* guide);
 /* set != 0: load params (host, TURNER_GUIDE_PARAMS floats); 0: read them. */
@@ -429,12 +434,23 @@ int turner_guide_forward(turner_guide* guide, const float* features, uint32_t n,
 /* Sum over samples of d(-w log q)/d params into grad (host), and the summed loss. */
 int turner_guide_gradient(turner_guide* guide, const float* features, const float* dirs, const float* weights,
                           uint32_t n, float* grad, float* loss);
+/* Training objective of the proposal, for turner_guide_gradient, _train and
+ * online training. KL (default): loss -c log q(w) per sample, the gradient
+ * averaged over the samples. VARIANCE: the second moment of the estimator
+ * that samples the mixture p = q/2 + max(0, n.w)/(2 pi): per sample the
+ * gradient of -c' log q with c' = c^2 q(w) / (2 p(w)) held constant (n the
+ * normal of the sample's features), the step's gradient divided by the sum
+ * of its weights c'. */
+#define TURNER_GUIDE_OBJECTIVE_KL 0
+#define TURNER_GUIDE_OBJECTIVE_VARIANCE 1
+int turner_guide_set_objective(turner_guide* guide, int objective);
 /* `steps` Adam steps (learning rate lr) on one batch; *loss = mean loss of the last. */
 int turner_guide_train(turner_guide* guide, const float* features, const float* dirs, const float* weights,
                        uint32_t n, float lr, uint32_t steps, float* loss);
 
 /* Binds a proposal to the context for jobs with TURNER_SAMPLING_GUIDED
- * (guide may be NULL to unbind). train != 0: online training during
+ * (guide may be NULL to unbind; a proposal created on another context is
+ * rejected with TURNER_ERR_INVALID_ARG). train != 0: online training during
  * turner_render / turner_render_accumulate: after every pass (chunk), the
  * pass's recorded bounces (about records_per_pass of them, >= 128; 0 keeps
  * the current value, default 2^18) get their target weight (incident

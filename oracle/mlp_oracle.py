@@ -11,7 +11,11 @@ against the GPU kernels (tests/test_gpu_guide.py).
   hidden  4 x 64 ReLU;  output 40 = 8 lobes x (direction, log kappa, logit)
   head    q(w) = sum_l softmax(logit)_l vMF(w; mu_l, kappa_l),
           mu_l = d_l / |d_l|, kappa_l = exp(clip(r_l, -3, 5)) + 1e-3
-  loss    mean over samples of -c_i log q(w_i)
+  loss    mean over samples of -c_i log q(w_i) (objective "kl"); objective
+          "variance": -c'_i log q(w_i) with c' = c^2 q / (2 p) held constant,
+          p = q/2 + max(0, n.w)/(2 pi) the sampling mixture and n the normal
+          of the features: the gradient of sum c^2 p0 / p(params) at p0 = p,
+          the second moment of the mixture estimator (variance_objective)
 With bf16=True the GPU's roundings are applied: weights, the encoded input
 and hidden activations to BF16; every layer's output gradient dY to BF16,
 as it enters the tensor-core products dY W, dY^T X and the bias sums.
@@ -107,9 +111,34 @@ def mixture_pdf(raw: np.ndarray, dirs: np.ndarray) -> np.ndarray:
     return (w * vmf_pdf(mu, kappa, dirs)).sum(axis=1)
 
 
-def loss_sum(p, feat, dirs, c, use_bf16=False) -> float:
+def variance_weights(raw, feat, dirs, c) -> np.ndarray:
+    """c' = c^2 q / (2 p), p = q/2 + max(0, n.w)/(2 pi) (guide.cu head_grad)."""
+    q = np.maximum(mixture_pdf(raw, dirs), 1e-20)
+    cw = np.maximum((np.asarray(feat, np.float64)[:, 3:6] * dirs).sum(axis=1), 0.0)
+    pm = 0.5 * q + 0.5 * cw / np.pi
+    return c * c * (0.5 * q / pm)
+
+
+def sampling_pdf(p, feat, dirs, use_bf16=False) -> np.ndarray:
+    """The mixture p = q/2 + max(0, n.w)/(2 pi) the renderer samples."""
     raw, _ = forward(p, feat, use_bf16)
     q = np.maximum(mixture_pdf(raw, dirs), 1e-20)
+    cw = np.maximum((np.asarray(feat, np.float64)[:, 3:6] * dirs).sum(axis=1), 0.0)
+    return 0.5 * q + 0.5 * cw / np.pi
+
+
+def variance_objective(p, feat, dirs, c, p0) -> float:
+    """sum c^2 p0 / p(params): with c = F / p0 the estimator's second moment
+    over samples drawn from p0; its gradient at p = p0 is the variance
+    objective's gradient."""
+    return float(np.sum(c * c * p0 / sampling_pdf(p, feat, dirs)))
+
+
+def loss_sum(p, feat, dirs, c, use_bf16=False, objective="kl") -> float:
+    raw, _ = forward(p, feat, use_bf16)
+    q = np.maximum(mixture_pdf(raw, dirs), 1e-20)
+    if objective == "variance":
+        c = variance_weights(raw, feat, dirs, c)
     return float(np.sum(-c * np.log(q)))
 
 
@@ -133,12 +162,17 @@ def head_grad(raw: np.ndarray, dirs: np.ndarray, c: np.ndarray) -> np.ndarray:
     return g.reshape(-1, OUT)
 
 
-def gradient(p, feat, dirs, c, use_bf16=False) -> np.ndarray:
-    """Analytic d(sum_i -c_i log q_i)/d params, same layout as the params."""
+def gradient(p, feat, dirs, c, use_bf16=False, objective="kl") -> np.ndarray:
+    """Analytic d(sum_i -c_i log q_i)/d params, same layout as the params
+    (objective "variance": with the weights c' of variance_weights)."""
     p = np.asarray(p, np.float64)
     raw, xs = forward(p, feat, use_bf16)
     layers = unpack(p)
-    dy = head_grad(raw, np.asarray(dirs, np.float64), np.asarray(c, np.float64))
+    dirs = np.asarray(dirs, np.float64)
+    c = np.asarray(c, np.float64)
+    if objective == "variance":
+        c = variance_weights(raw, feat, dirs, c)
+    dy = head_grad(raw, dirs, c)
     grads = [None] * 5
     for l in range(4, -1, -1):
         W, _ = layers[l]

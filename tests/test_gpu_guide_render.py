@@ -42,6 +42,34 @@ def test_guided_sampling_requires_a_guide(setup):
         ctx.render([job(tg.SAMPLING_GUIDED, 1, 1)])
 
 
+def test_guide_and_context_destroy_in_either_order(setup):
+    """Destroying a bound proposal unbinds it; a proposal whose context was
+    destroyed first refuses every call but its own destroy; a proposal is
+    bound only to the context that created it."""
+    ctx, job, _ = setup
+    g = tg.Guide(ctx, seed=5)
+    ctx.set_guide(g, train=False)
+    ctx.render([job(tg.SAMPLING_GUIDED, 1, 1)])
+    g.close()
+    with pytest.raises(tg.TurnerError) as e:   # no proposal bound any more
+        ctx.render([job(tg.SAMPLING_GUIDED, 1, 1)])
+    assert e.value.status == tg.ERR_INVALID_ARG
+    other = tg.Context(0)
+    g2 = tg.Guide(other, seed=6)
+    with pytest.raises(tg.TurnerError) as e:
+        ctx.set_guide(g2)
+    assert e.value.status == tg.ERR_INVALID_ARG
+    other.set_guide(g2, train=False)
+    params = g2.get_params()
+    other.close()
+    with pytest.raises(tg.TurnerError) as e:
+        g2.get_params()
+    assert e.value.status == tg.ERR_INVALID_ARG
+    with pytest.raises(tg.TurnerError):
+        g2.set_params(params)
+    g2.close()
+
+
 def test_untrained_proposal_is_unbiased(setup):
     """Any network output keeps the estimator unbiased (cosine floor weight 1/2)."""
     ctx, job, ref = setup

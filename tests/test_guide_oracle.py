@@ -62,6 +62,24 @@ def test_network_gradient_matches_finite_differences():
         assert abs(fd - g[k]) <= 1e-4 * max(1.0, abs(fd)), (k, fd, g[k])
 
 
+def test_variance_gradient_matches_finite_differences():
+    """The variance objective's per-sample weights c' = c^2 q / (2 p) make
+    -c' d log q the gradient of sum c^2 p0 / p, the mixture estimator's second
+    moment over samples drawn from p0, at p = p0."""
+    p = mo.init_params(17) + np.random.default_rng(18).normal(size=mo.n_params()) * 0.01
+    feat, d, c = _batch(16, 19)
+    p0 = mo.sampling_pdf(p, feat, d)
+    g = mo.gradient(p, feat, d, c, objective="variance")
+    rng = np.random.default_rng(20)
+    eps = 1e-6
+    for k in rng.choice(mo.n_params(), 60, replace=False):
+        pp, pm = p.copy(), p.copy()
+        pp[k] += eps
+        pm[k] -= eps
+        fd = (mo.variance_objective(pp, feat, d, c, p0) - mo.variance_objective(pm, feat, d, c, p0)) / (2 * eps)
+        assert abs(fd - g[k]) <= 1e-4 * max(1.0, abs(fd)), (k, fd, g[k])
+
+
 def test_bf16_rounding():
     x = np.array([1.0, 1.00390625, 1.005859375, -3.3e-5, 65504.0])
     r = mo.bf16(x)

@@ -129,6 +129,7 @@ def _lib() -> C.CDLL:
         "turner_set_graph_mode": (C.c_int, [_P, C.c_int]),
         "turner_autotune": (C.c_int, [_P, C.POINTER(Job), C.c_uint32, C.c_int, C.POINTER(Tuning)]),
         "turner_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+        "turner_guide_set_objective": (C.c_int, [_P, C.c_int]),
         "turner_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
         "turner_graph_launch_count": (C.c_uint64, [_P]),
         "turner_set_traversal_launch": (C.c_int, [_P, C.c_int, C.c_uint32]),
@@ -581,6 +582,7 @@ class Context:
 
 
 GUIDE_PARAMS = 20264
+GUIDE_OBJECTIVE_KL, GUIDE_OBJECTIVE_VARIANCE = 0, 1
 
 
 class Guide:
@@ -602,6 +604,10 @@ class Guide:
     @property
     def handle(self) -> int:
         return self._h.value
+
+    def set_objective(self, objective: int) -> None:
+        """GUIDE_OBJECTIVE_KL (default) or GUIDE_OBJECTIVE_VARIANCE (the 50/50 estimator's second moment)."""
+        _check(_lib().turner_guide_set_objective(self._h, objective), "turner_guide_set_objective")
 
     def get_params(self) -> np.ndarray:
         p = np.empty(GUIDE_PARAMS, np.float32)

@@ -94,8 +94,10 @@ struct turner_ctx {
     int graph_mode = TURNER_GRAPH_AUTO;
     cudaGraphExec_t graph_exec = nullptr;   // last instantiated batch graph, updated in place when it can be
     uint64_t graph_updates = 0;
-    // learned proposal used by jobs with TURNER_SAMPLING_GUIDED
+    // learned proposal used by jobs with TURNER_SAMPLING_GUIDED, and every
+    // live proposal created on this context (they share its stream)
     turner_guide* guide = nullptr;
+    std::vector<turner_guide*> guides;
     bool guide_train = false;
     float guide_lr = 1e-3f;
     uint32_t guide_records = 1u << 18;   // training samples per pass
@@ -331,6 +333,11 @@ void turner_destroy(turner_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    // proposals that outlive their context lose its stream: afterwards they
+    // accept turner_guide_destroy only
+    for (turner_guide* g : ctx->guides) turner::guide::orphan(g);
+    ctx->guides.clear();
+    ctx->guide = nullptr;
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     ctx->scenes.clear();
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -347,6 +354,14 @@ int turner_last_device_error(turner_ctx* ctx) { return ctx ? TURNER_OK : TURNER_
 namespace turner {
 cudaStream_t ctx_stream(turner_ctx* ctx) { return ctx->stream; }
 int ctx_device(turner_ctx* ctx) { return ctx->device; }
+void ctx_add_guide(turner_ctx* ctx, turner_guide* g) { ctx->guides.push_back(g); }
+void ctx_remove_guide(turner_ctx* ctx, turner_guide* g) {
+    ctx->guides.erase(std::remove(ctx->guides.begin(), ctx->guides.end(), g), ctx->guides.end());
+    if (ctx->guide == g) {
+        ctx->guide = nullptr;
+        ctx->guide_train = false;
+    }
+}
 } // namespace turner
 
 extern "C" {
@@ -1290,6 +1305,7 @@ int turner_autotune(turner_ctx* ctx, const turner_job* jobs, uint32_t n_jobs, in
 
 int turner_set_guide(turner_ctx* ctx, turner_guide* guide, int train, float lr, uint32_t records_per_pass) {
     if (!ctx || (train && !guide) || !(lr >= 0.f) || (train && records_per_pass < 128)) return TURNER_ERR_INVALID_ARG;
+    if (guide && turner::guide::owner(guide) != ctx) return TURNER_ERR_INVALID_ARG;
     ctx->guide = guide;
     ctx->guide_train = train != 0 && guide;
     ctx->guide_lr = lr;

@@ -295,6 +295,7 @@ struct BwdSmem {
     int abort;
     int last;
     float loss;
+    float wsum;   // sum of the tile weights c' (variance objective)
 };
 
 // Per-step training state, resident on the device so that a training step
@@ -308,6 +309,7 @@ struct TrainState {
     float scale;       // 1 / n (the loss is a mean over samples)
     float loss_mean;   // loss of the last step / n
     uint32_t done;     // backward CTAs finished in this step (the last one updates)
+    float wsum;        // variance objective: sum of the step's weights c' (the gradient is divided by it)
 };
 
 struct AdamArgs {
@@ -320,8 +322,15 @@ struct AdamArgs {
     float lr, b1, b2, eps;
 };
 
-// Head gradient of L = -c log q(w): writes dL/d raw (40) and returns L.
-__device__ __forceinline__ float head_grad(const float raw[kOut], const float dir[3], float c, float g[kOut]) {
+// Head gradient of L = -c' log q(w): writes dL/d raw (40), returns L and
+// the weight c' used. Objective 0 (KL divergence): c' = c. Objective 1
+// (variance of the sampling mixture p = q/2 + max(0, n.w)/(2 pi)): c' =
+// c^2 q / (2 p), held constant; with c = F / p the sample's integrand over
+// its pdf, -c' d log q is the gradient of F^2 / p, whose expectation is the
+// estimator's second moment (Mueller et al., "Neural Importance Sampling",
+// 2019, the chi-square divergence, with the cosine half of the mixture).
+__device__ __forceinline__ float head_grad(const float raw[kOut], const float dir[3], float c, const float nrm[3],
+                                           int objective, float g[kOut], float& c_used) {
     Mixture m;
     decode(raw, m);
     float p[kLobes], q = 0.f;
@@ -331,6 +340,12 @@ __device__ __forceinline__ float head_grad(const float raw[kOut], const float di
         q += m.w[l] * p[l];
     }
     q = fmaxf(q, 1e-20f);
+    if (objective == kObjectiveVariance) {
+        const float cw = fmaxf(nrm[0] * dir[0] + nrm[1] * dir[1] + nrm[2] * dir[2], 0.f);
+        const float pm = 0.5f * q + 0.5f * cw * kInvPi;
+        c = c * c * (0.5f * q / pm);
+    }
+    c_used = c;
     const float loss = -c * logf(q);
     const float gq = -c / q;
     float gw[kLobes], wg = 0.f;
@@ -438,12 +453,16 @@ __device__ __forceinline__ void issue_steps(uint32_t tmem, const uint8_t* a, con
 }
 
 // features/acts/out as produced by k_mlp_forward for the same samples;
-// dirs: n x 3 unit directions; weight: n target weights c. grad += dLoss/dparams;
-// with do_adam, the last CTA then takes the Adam step (see above).
+// dirs: n x 3 unit directions; weight: n target weights c; feat: the n x 9
+// features (their normals enter the variance objective). grad +=
+// dLoss/dparams; with do_adam, the last CTA then takes the Adam step (see
+// above), on the gradient over n (KL objective) or over the sum of the
+// weights c' (variance objective).
 __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     uint32_t n, const uint32_t* __restrict__ n_dev, const __nv_bfloat16* __restrict__ acts,
-    const float* __restrict__ out, const float* __restrict__ dirs, const float* __restrict__ weight, Weights wts,
-    float* __restrict__ grad, float* __restrict__ loss_sum, int* err, AdamArgs adam, int do_adam) {
+    const float* __restrict__ out, const float* __restrict__ dirs, const float* __restrict__ weight,
+    const float* __restrict__ feat, int objective, Weights wts, float* __restrict__ grad,
+    float* __restrict__ loss_sum, int* err, AdamArgs adam, int do_adam) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -459,6 +478,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
         sm.abort = 0;
         sm.last = 0;
         sm.loss = 0.f;
+        sm.wsum = 0.f;
         tc::mbar_init(&sm.mbar, 1);
         tc::fence_mbar_init();
     }
@@ -472,7 +492,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     const uint32_t lane_base = (quad * 32u) << 16;
     uint32_t phase = 0;
     const uint32_t tiles = (n + 127) / 128;
-    float my_loss = 0.f;
+    float my_loss = 0.f, my_w = 0.f;
     bool had_tile = false;
 
     int cur = 0;   // xrow buffer holding the current X
@@ -499,7 +519,14 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
                     raw[4 * q + 3] = v.w;
                 }
                 const float d[3] = {dirs[3 * size_t(s)], dirs[3 * size_t(s) + 1], dirs[3 * size_t(s) + 2]};
-                my_loss += head_grad(raw, d, weight[s], g);
+                float nrm[3] = {0.f, 0.f, 0.f};
+                if (objective == kObjectiveVariance) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) nrm[k] = feat[9 * size_t(s) + 3 + k];
+                }
+                float cu;
+                my_loss += head_grad(raw, d, weight[s], nrm, objective, g, cu);
+                my_w += cu;
             } else {
 #pragma unroll
                 for (int k = 0; k < kOut; ++k) g[k] = 0.f;
@@ -574,8 +601,14 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     }
     cp_async_wait_all();   // no copy may outlive the kernel (an abort can leave one in flight)
     // loss, and this CTA's dW' out of TMEM into the global gradient
-    for (int off = 16; off > 0; off >>= 1) my_loss += __shfl_xor_sync(0xFFFFFFFFu, my_loss, off);
-    if (lane == 0) atomicAdd(&sm.loss, my_loss);
+    for (int off = 16; off > 0; off >>= 1) {
+        my_loss += __shfl_xor_sync(0xFFFFFFFFu, my_loss, off);
+        my_w += __shfl_xor_sync(0xFFFFFFFFu, my_w, off);
+    }
+    if (lane == 0) {
+        atomicAdd(&sm.loss, my_loss);
+        atomicAdd(&sm.wsum, my_w);
+    }
     if (sm.abort && tid == 0) tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
     tc::tc_fence_before_sync();
     __syncthreads();
@@ -604,6 +637,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     if (warp == 0) tc::tmem_dealloc(tmem, kBwdTmemCols);
     if (tid == 0 && loss_sum) atomicAdd(loss_sum, sm.loss);
     if (!do_adam) return;
+    if (tid == 0) atomicAdd(&adam.state->wsum, sm.wsum);
     // the last CTA to finish takes the Adam step on the complete gradient
     __threadfence();
     __syncthreads();
@@ -613,7 +647,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
     __threadfence();
     TrainState* st = adam.state;
     if (!st->skip) {
-        const float scale = st->scale, bc1 = st->bc1, bc2 = st->bc2;
+        const float scale = objective == kObjectiveVariance ? 1.f / fmaxf(__ldcg(&st->wsum), 1e-30f) : st->scale;
+        const float bc1 = st->bc1, bc2 = st->bc2;
         for (int i = tid; i < kParams; i += kBwdThreads) {
             const float gi = __ldcg(grad + i) * scale;
             const float mi = adam.b1 * adam.m[i] + (1.f - adam.b1) * gi;
@@ -656,6 +691,7 @@ __global__ void k_train_prep(const uint32_t* __restrict__ n_dev, uint32_t n, uin
     s->n = n;
     s->skip = n < min_n ? 1 : 0;
     s->done = 0;
+    s->wsum = 0.f;
     if (s->skip) return;
     s->step += 1;
     s->bc1 = 1.f - powf(b1, static_cast<float>(s->step));
@@ -709,6 +745,7 @@ struct turner_guide {
     float* out = nullptr;
     __nv_bfloat16* acts = nullptr;
     bool grad_dirty = false;   // grad / loss hold a turner_guide_gradient result, not zeros
+    int objective = kObjectiveKL;   // training objective (turner_guide_set_objective)
     int sms = 1;
     double train_ms = 0, infer_ms = 0;
     uint64_t train_steps = 0;
@@ -844,8 +881,9 @@ int train_device(turner_guide* g, const float* feat, const float* dirs, const fl
     k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), stream>>>(n, n_step, feat, w, g->out, g->acts,
                                                                              g->err);
     const AdamArgs adam{g->params, g->m, g->v, g->fwd, g->bwd, g->state, lr, b1, b2, 1e-8f};
-    k_mlp_backward<<<grid_tiles(g, n), kBwdThreads, bwd_smem(), stream>>>(n, n_step, g->acts, g->out, dirs, wts, w,
-                                                                         g->grad, g->loss, g->err, adam, 1);
+    k_mlp_backward<<<grid_tiles(g, n), kBwdThreads, bwd_smem(), stream>>>(n, n_step, g->acts, g->out, dirs, wts, feat,
+                                                                         g->objective, w, g->grad, g->loss, g->err,
+                                                                         adam, 1);
     GCK(cudaGetLastError());
     g->train_steps += 1;
     if (loss_out) {
@@ -855,6 +893,13 @@ int train_device(turner_guide* g, const float* feat, const float* dirs, const fl
         *loss_out = s.loss_mean;
     }
     return TURNER_OK;
+}
+
+turner_ctx* owner(const turner_guide* g) { return g->ctx; }
+
+void orphan(turner_guide* g) {
+    g->ctx = nullptr;
+    g->stream = nullptr;
 }
 
 int train_state(turner_guide* g, uint64_t* steps, float* last_loss) {
@@ -872,6 +917,8 @@ int train_state(turner_guide* g, uint64_t* steps, float* last_loss) {
 namespace turner {
 cudaStream_t ctx_stream(turner_ctx* ctx);
 int ctx_device(turner_ctx* ctx);
+void ctx_add_guide(turner_ctx* ctx, turner_guide* g);
+void ctx_remove_guide(turner_ctx* ctx, turner_guide* g);
 } // namespace turner
 
 extern "C" {
@@ -941,6 +988,7 @@ int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
         turner_guide_destroy(g);
         return cuda_status(e);
     }
+    turner::ctx_add_guide(ctx, g);
     *out = g;
     return TURNER_OK;
 }
@@ -948,7 +996,9 @@ int turner_guide_create(turner_ctx* ctx, uint64_t seed, turner_guide** out) {
 void turner_guide_destroy(turner_guide* g) {
     if (!g) return;
     cudaSetDevice(g->device);
+    if (g->ctx) turner::ctx_remove_guide(g->ctx, g);   // unbinds it where it is the context's proposal
     if (g->stream) cudaStreamSynchronize(g->stream);
+    else cudaDeviceSynchronize();   // orphaned: the context's stream is gone
     for (void* p : {static_cast<void*>(g->params), static_cast<void*>(g->m), static_cast<void*>(g->v),
                     static_cast<void*>(g->grad), static_cast<void*>(g->fwd), static_cast<void*>(g->bwd),
                     static_cast<void*>(g->loss), static_cast<void*>(g->err), static_cast<void*>(g->feat),
@@ -960,7 +1010,7 @@ void turner_guide_destroy(turner_guide* g) {
 }
 
 int turner_guide_params(turner_guide* g, float* host, int set) {
-    if (!g || !host) return TURNER_ERR_INVALID_ARG;
+    if (!g || !g->ctx || !host) return TURNER_ERR_INVALID_ARG;
     cudaSetDevice(g->device);
     if (set) {
         GCK(cudaMemcpyAsync(g->params, host, kParams * sizeof(float), cudaMemcpyHostToDevice, g->stream));
@@ -973,8 +1023,14 @@ int turner_guide_params(turner_guide* g, float* host, int set) {
     return TURNER_OK;
 }
 
+int turner_guide_set_objective(turner_guide* g, int objective) {
+    if (!g || !g->ctx || (objective != kObjectiveKL && objective != kObjectiveVariance)) return TURNER_ERR_INVALID_ARG;
+    g->objective = objective;
+    return TURNER_OK;
+}
+
 int turner_guide_forward(turner_guide* g, const float* features, uint32_t n, float* out) {
-    if (!g || !features || !out) return TURNER_ERR_INVALID_ARG;
+    if (!g || !g->ctx || !features || !out) return TURNER_ERR_INVALID_ARG;
     if (n == 0) return TURNER_OK;
     cudaSetDevice(g->device);
     int st = ensure_batch(g, n);
@@ -989,7 +1045,7 @@ int turner_guide_forward(turner_guide* g, const float* features, uint32_t n, flo
 
 int turner_guide_gradient(turner_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
                           float* grad_out, float* loss_out) {
-    if (!g || !features || !dirs || !weights || !grad_out || n == 0) return TURNER_ERR_INVALID_ARG;
+    if (!g || !g->ctx || !features || !dirs || !weights || !grad_out || n == 0) return TURNER_ERR_INVALID_ARG;
     cudaSetDevice(g->device);
     int st = ensure_batch(g, n);
     if (st != TURNER_OK) return st;
@@ -1002,8 +1058,8 @@ int turner_guide_gradient(turner_guide* g, const float* features, const float* d
     Weights w{g->fwd, g->bwd, g->params};
     k_mlp_forward<<<grid_tiles_fwd(g, n), kFwdThreads, fwd_smem(), g->stream>>>(n, nullptr, g->feat, w, g->out, g->acts, g->err);
     k_mlp_backward<<<grid_tiles(g, n), kBwdThreads, bwd_smem(), g->stream>>>(n, nullptr, g->acts, g->out, g->dirs,
-                                                                            g->wts, w, g->grad, g->loss, g->err,
-                                                                            AdamArgs{}, 0);
+                                                                            g->wts, g->feat, g->objective, w, g->grad,
+                                                                            g->loss, g->err, AdamArgs{}, 0);
     GCK(cudaGetLastError());
     GCK(cudaMemcpyAsync(grad_out, g->grad, kParams * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     float l = 0;
@@ -1015,7 +1071,7 @@ int turner_guide_gradient(turner_guide* g, const float* features, const float* d
 
 int turner_guide_train(turner_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
                        float lr, uint32_t steps, float* loss_out) {
-    if (!g || !features || !dirs || !weights || n == 0) return TURNER_ERR_INVALID_ARG;
+    if (!g || !g->ctx || !features || !dirs || !weights || n == 0) return TURNER_ERR_INVALID_ARG;
     cudaSetDevice(g->device);
     int st = ensure_batch(g, n);
     if (st != TURNER_OK) return st;

@@ -81,6 +81,8 @@ struct Mixture {
 constexpr float kKappaRawMin = -3.f, kKappaRawMax = 5.f, kKappaFloor = 1e-3f;
 constexpr float kInvTwoPi = 0.159154943091895335769f;
 constexpr float kInvPi = 0.318309886183790671538f;
+// training objectives of the proposal (turner_guide_set_objective)
+constexpr int kObjectiveKL = 0, kObjectiveVariance = 1;
 
 __device__ __forceinline__ void decode(const float raw[kOut], Mixture& m) {
     float mx = -1e30f;

@@ -164,6 +164,7 @@ void launch_accumulate(const JobDesc* jobs, uint32_t n_jobs, const Chunk& c, con
 } // namespace turner
 
 struct turner_guide;
+struct turner_ctx;
 
 namespace turner {
 namespace guide {
@@ -181,5 +182,10 @@ int train_device(turner_guide* g, const float* feat, const float* dirs, const fl
                  const uint32_t* n_dev, uint32_t min_n, float lr, cudaStream_t stream, float* loss_out);
 // Adam steps taken and the last step's mean loss (waits for the stream).
 int train_state(turner_guide* g, uint64_t* steps, float* last_loss);
+// The context a proposal was created on (null once that context is destroyed).
+turner_ctx* owner(const turner_guide* g);
+// Called by turner_destroy for each proposal still alive: drops the context
+// and its stream, so that the proposal accepts turner_guide_destroy only.
+void orphan(turner_guide* g);
 } // namespace guide
 } // namespace turner
