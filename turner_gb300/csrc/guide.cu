@@ -35,7 +35,6 @@
 namespace turner {
 namespace guide {
 
-constexpr uint32_t kTmemCols = 64;
 
 struct Weights {
     const uint8_t* fwd;      // packed BF16 forward operands (kFwdBytes)
@@ -62,51 +61,74 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, const uint8_t* a, con
 }
 
 // ---------------------------------------------------------------- forward
-constexpr int kFwdThreads = 256;   // two warps per TMEM lane quadrant
-constexpr int kFwdBlocksPerSm = 3;
+// One persistent CTA per SM runs kFwdGroups independent tile pipelines, one
+// per warpgroup: the warpgroup's thread t owns row t of its 128-sample tile,
+// its own activation buffer, 64 TMEM columns and mbarrier, and syncs on its
+// own named barrier, so that one group's MMAs run while the others' epilogues
+// (TMEM read-back, bias, ReLU, BF16 packing) do. The packed weights are
+// loaded once per SM and shared by the groups.
+constexpr int kFwdGroups = 6;
+constexpr int kFwdThreads = 128 * kFwdGroups;
+constexpr uint32_t kFwdTmemCols = 512;   // kFwdGroups x 64 columns, allocated as a power of two
+static_assert(kFwdGroups * 64 <= static_cast<int>(kFwdTmemCols), "TMEM columns");
 
 struct FwdSmem {
+    uint8_t act[kFwdGroups][kIn * 128 * 2];   // per group: 128 x 80 inputs, then each layer's 128 x 64 output in place
     uint8_t w[kFwdBytes];
-    uint8_t act[kIn * 128 * 2];        // 128 x 80 inputs, then each layer's 128 x 64 output in place
     float bias[4 * kHidden + kOut];
-    uint64_t mbar;
+    uint64_t mbar[kFwdGroups];
     uint32_t tmem;
-    int abort;
 };
+
+// Barrier `id` over the 128 threads of one warpgroup; returns whether any of
+// them passed a non-zero `pred`.
+__device__ __forceinline__ int group_sync_or(int id, int pred) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "barrier.cta.red.or.pred q, %2, 128, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"(pred), "r"(id)
+        : "memory");
+    return r;
+}
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Eight encoded inputs k = 8g .. 8g + 7 of one sample (see encode()): groups
-// 0-8 are four frequencies of one axis, group 9 the normal, albedo and padding.
-// The group's first frequency comes from sincospif, the next three from the
-// double-angle identities sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)
-// (cos a + sin a): three doublings grow the FP32 error by at most 8x, far
-// below the BF16 rounding of the stored value (2^-9).
-__device__ __forceinline__ uint4 encode_group(int g, const float p[3], const float nn[3], const float a[3]) {
-    float f[8];
-    if (g < 9) {
-        const int ax = g / 3, i0 = (g - ax * 3) * 4;
-        const float x = g < 3 ? p[0] : g < 6 ? p[1] : p[2];
-        float sn, cs;
-        sincospif(x * static_cast<float>(1 << i0), &sn, &cs);
+// Two FP32 values as BF16 (round to nearest even), max(x, 0) applied:
+// lo in the low half, hi in the high half.
+__device__ __forceinline__ uint32_t pack_bf16x2_relu(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+// The 24 encoded inputs of one coordinate (see encode()): (sin, cos) of
+// pi 2^i x for i = 0..11, as three groups of eight BF16. One sincospif, then
+// the double-angle identities sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)
+// (cos a + sin a): eleven doublings grow the FP32 error to at most 2^11 times
+// sincospif's (about 1e-4), a twentieth of the BF16 rounding of the stored
+// value (2^-9).
+__device__ __forceinline__ void encode_axis(float x, uint4 out[3]) {
+    float sn, cs;
+    sincospif(x, &sn, &cs);
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+        uint32_t w[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            f[2 * j] = sn;
-            f[2 * j + 1] = cs;
+            w[j] = pack_bf16x2(sn, cs);
             const float s2 = 2.f * sn * cs;
             cs = (cs - sn) * (cs + sn);
             sn = s2;
         }
-    } else {
-        f[0] = nn[0]; f[1] = nn[1]; f[2] = nn[2];
-        f[3] = a[0]; f[4] = a[1]; f[5] = a[2];
-        f[6] = 0.f; f[7] = 0.f;
+        out[g] = make_uint4(w[0], w[1], w[2], w[3]);
     }
-    return make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
-                      pack_bf16x2(f[6], f[7]));
 }
 
 // features: n x 9 floats (position in [0,1]^3, shading normal, albedo).
@@ -115,19 +137,18 @@ __device__ __forceinline__ uint4 encode_group(int g, const float p[3], const flo
 // n_dev (optional): the sample count is read from device memory (a queue
 // length), capped at n.
 //
-// Thread t works on row t % 128 of the tile; the two threads of a row split
-// its input groups (5 each) and its output columns (32 each for hidden
-// layers; 32 and 16 of the padded 48 for the head), so every shared-memory
-// write is one 16-byte store of 8 BF16 values. A layer's output overwrites
-// its input in place: the MMAs have read it once their commit has arrived.
-__global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
+// Group g of CTA b takes tiles b * kFwdGroups + g, then every gridDim.x *
+// kFwdGroups-th. Every shared-memory write is one 16-byte store of 8 BF16
+// values of the thread's row. A layer's output overwrites its input in
+// place: the MMAs have read it once their commit has arrived.
+__global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
     uint32_t n, const uint32_t* __restrict__ n_dev, const float* __restrict__ features, Weights wts,
     float* __restrict__ out, __nv_bfloat16* __restrict__ acts, int* err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     FwdSmem& sm = *reinterpret_cast<FwdSmem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int grp = tid >> 7;
     const uint32_t row = static_cast<uint32_t>(tid & 127);
-    const int half = tid >> 7;
     if (n_dev) n = min(n, *n_dev);
     for (int i = tid; i < kFwdBytes / 16; i += kFwdThreads) {
         reinterpret_cast<uint4*>(sm.w)[i] = reinterpret_cast<const uint4*>(wts.fwd)[i];
@@ -136,20 +157,25 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
         for (int i = tid; i < layer_out(l); i += kFwdThreads) sm.bias[o + i] = wts.params[layer_b(l) + i];
         o += layer_out(l);
     }
-    if (tid == 0) {
-        sm.abort = 0;
-        tc::mbar_init(&sm.mbar, 1);
+    if (tid < kFwdGroups) {
+        tc::mbar_init(&sm.mbar[tid], 1);
         tc::fence_mbar_init();
     }
-    if (warp == 0) tc::tmem_alloc(&sm.tmem, kTmemCols);
+    if (warp == 0) tc::tmem_alloc(&sm.tmem, kFwdTmemCols);
     tc::fence_async_smem();
     tc::tc_fence_before_sync();
     __syncthreads();
     tc::tc_fence_after_sync();
-    const uint32_t tmem = sm.tmem;
-    const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;
+    // this group's accumulator: TMEM lanes 0-127 (warp w of the group reads
+    // lanes 32w..32w+31), columns 64 grp .. 64 grp + 63
+    const uint32_t tmem = sm.tmem + static_cast<uint32_t>(grp * 64) + (static_cast<uint32_t>(warp & 3) * 32u << 16);
+    const uint32_t tmem_mma = sm.tmem + static_cast<uint32_t>(grp * 64);
+    uint8_t* const act = sm.act[grp];
+    uint64_t* const mbar = &sm.mbar[grp];
+    const int bar_id = 1 + grp;   // named barrier 0 is __syncthreads'
     uint32_t phase = 0;
     const uint32_t tiles = (n + 127) / 128;
+    const uint32_t stride = gridDim.x * kFwdGroups;
 
     // this row's 9 input floats; the next tile's are loaded while the
     // current tile runs through the layers
@@ -162,102 +188,107 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdBlocksPerSm) k_mlp_forward(
             for (int k = 0; k < 9; ++k) fin[k] = q[k];
         }
     };
-    load_features(blockIdx.x);
-    bool aborted = false;   // the same in every thread: set after a barrier
-    for (uint32_t tile = blockIdx.x; tile < tiles && !aborted; tile += gridDim.x) {
+    const uint32_t first = blockIdx.x * kFwdGroups + static_cast<uint32_t>(grp);
+    load_features(first);
+    bool aborted = false;   // the same in every thread of the group: set after a group barrier
+    for (uint32_t tile = first; tile < tiles && !aborted; tile += stride) {
         const uint32_t s = tile * 128 + row;
         const bool valid = s < n;
         uint4* const act_row = acts && valid ? reinterpret_cast<uint4*>(acts + size_t(s) * 336) : nullptr;
         {
-            const float p[3] = {fin[0], fin[1], fin[2]}, nn[3] = {fin[3], fin[4], fin[5]},
-                        a[3] = {fin[6], fin[7], fin[8]};
-#pragma unroll 1
-            for (int g = half * 5; g < half * 5 + 5; ++g) {
-                const uint4 v = valid ? encode_group(g, p, nn, a) : make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<uint4*>(sm.act + tc::kmajor_offset(row, 8 * g, kIn)) = v;
-                if (act_row) act_row[g] = v;
+            // groups 0-8: twelve frequencies of x, y, z (three independent
+            // chains, unrolled for ILP); group 9: normal, albedo, zero padding
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                uint4 v[3] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+                if (valid) encode_axis(ax == 0 ? fin[0] : ax == 1 ? fin[1] : fin[2], v);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 8 * (3 * ax + j), kIn)) = v[j];
+                    if (act_row) act_row[3 * ax + j] = v[j];
+                }
             }
+            const uint4 v = valid ? make_uint4(pack_bf16x2(fin[3], fin[4]), pack_bf16x2(fin[5], fin[6]),
+                                               pack_bf16x2(fin[7], fin[8]), 0u)
+                                  : make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 72, kIn)) = v;
+            if (act_row) act_row[9] = v;
         }
-        load_features(tile + gridDim.x);
+        load_features(tile + stride);
         tc::fence_async_smem();
         tc::tc_fence_before_sync();
-        __syncthreads();
+        group_sync_or(bar_id, 0);
         tc::tc_fence_after_sync();
 
         int bias_o = 0;
 #pragma unroll 1
         for (int l = 0; l < kLayers; ++l) {
             const int K = layer_in(l), N = layer_out_pad(l);
-            if (tid == 0) issue_layer(tmem, sm.act, sm.w + fwd_off(l), K, N, &sm.mbar);
-            // a wait that gives up still runs the epilogue (on whatever TMEM
-            // holds); the barrier at the end of the layer then aborts the
-            // whole CTA together
-            const bool timed_out = !tc::mbar_wait(&sm.mbar, phase, err);
+            // one thread issues the layer's MMAs and waits for their commit;
+            // the rest of the group waits at the barrier, without polling
+            bool done = true;
+            if (row == 0) {
+                issue_layer(tmem_mma, act, sm.w + fwd_off(l), K, N, mbar);
+                done = tc::mbar_wait(mbar, phase, err);
+            }
             phase ^= 1;
+            if (group_sync_or(bar_id, done ? 0 : 1)) {
+                aborted = true;   // the wait gave up: nothing is read from TMEM
+                break;
+            }
             tc::tc_fence_after_sync();
-            const uint32_t c0 = static_cast<uint32_t>(half * 32);
             if (l < kLayers - 1) {
-                float v[32];
-                tc::tmem_ld16(tmem + lane_base + c0, v);
-                tc::tmem_ld16(tmem + lane_base + c0 + 16u, v + 16);
-                const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
+#pragma unroll 1
+                for (int c0 = 0; c0 < kHidden; c0 += 32) {
+                    float v[32];
+                    tc::tmem_ld32(tmem + static_cast<uint32_t>(c0), v);
+                    const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float4 ba = b4[2 * q], bb = b4[2 * q + 1];
-                    const float bq[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
-                    float y[8];
+                    for (int q = 0; q < 4; ++q) {
+                        const float4 ba = b4[2 * q], bb = b4[2 * q + 1];
+                        const float bq[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
+                        float y[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) y[j] = fmaxf(v[8 * q + j] + bq[j], 0.f);
-                    const uint4 u = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]),
-                                               pack_bf16x2(y[4], y[5]), pack_bf16x2(y[6], y[7]));
-                    *reinterpret_cast<uint4*>(sm.act + tc::kmajor_offset(row, c0 + 8 * q, kHidden)) = u;
-                    if (act_row) act_row[10 + 8 * l + half * 4 + q] = u;
-                }
-            } else if (half == 0) {
-                float v[32];
-                tc::tmem_ld16(tmem + lane_base, v);
-                tc::tmem_ld16(tmem + lane_base + 16u, v + 16);
-                if (out && valid) {
-                    float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        o4[q] = make_float4(v[4 * q] + sm.bias[bias_o + 4 * q], v[4 * q + 1] + sm.bias[bias_o + 4 * q + 1],
-                                            v[4 * q + 2] + sm.bias[bias_o + 4 * q + 2],
-                                            v[4 * q + 3] + sm.bias[bias_o + 4 * q + 3]);
+                        for (int j = 0; j < 8; ++j) y[j] = v[8 * q + j] + bq[j];
+                        const uint4 u = make_uint4(pack_bf16x2_relu(y[0], y[1]), pack_bf16x2_relu(y[2], y[3]),
+                                                   pack_bf16x2_relu(y[4], y[5]), pack_bf16x2_relu(y[6], y[7]));
+                        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, c0 + 8 * q, kHidden)) = u;
+                        if (act_row) act_row[10 + 8 * l + c0 / 8 + q] = u;
                     }
                 }
             } else {
-                float v[16];
-                tc::tmem_ld16(tmem + lane_base + 32u, v);
-                if (out && valid) {
-                    float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut + 32);
+#pragma unroll 1
+                for (int c0 = 0; c0 < kOut; c0 += 16) {
+                    float v[16];
+                    tc::tmem_ld16(tmem + static_cast<uint32_t>(c0), v);   // columns 40-47 are padding
+                    if (out && valid) {
+                        float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut + c0);
+                        const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        o4[q] = make_float4(v[4 * q] + sm.bias[bias_o + 32 + 4 * q],
-                                            v[4 * q + 1] + sm.bias[bias_o + 32 + 4 * q + 1],
-                                            v[4 * q + 2] + sm.bias[bias_o + 32 + 4 * q + 2],
-                                            v[4 * q + 3] + sm.bias[bias_o + 32 + 4 * q + 3]);
+                        for (int q = 0; q < 4; ++q) {
+                            if (c0 + 4 * q < kOut) {
+                                const float4 b = b4[q];
+                                o4[q] = make_float4(v[4 * q] + b.x, v[4 * q + 1] + b.y, v[4 * q + 2] + b.z,
+                                                    v[4 * q + 3] + b.w);
+                            }
+                        }
                     }
                 }
             }
             bias_o += layer_out(l);
-            tc::fence_async_smem();
+            tc::fence_async_smem();   // the next layer's MMAs read what this one wrote
             tc::tc_fence_before_sync();
-            const int any_timeout = __syncthreads_or(timed_out ? 1 : 0);
+            group_sync_or(bar_id, 0);
             tc::tc_fence_after_sync();
-            if (any_timeout) {
-                aborted = true;
-                break;
-            }
         }
     }
-    if (aborted && tid == 0) {
+    if (aborted && row == 0) {
         // drain: an MMA may still be in flight; wait once more (bounded)
-        tc::mbar_wait(&sm.mbar, phase ^ 1, nullptr, 1000000u);
+        tc::mbar_wait(mbar, phase ^ 1, nullptr, 1000000u);
     }
     tc::tc_fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::tmem_dealloc(sm.tmem, kFwdTmemCols);
 }
 
 // ---------------------------------------------------------------- backward
@@ -798,9 +829,10 @@ unsigned grid_tiles(turner_guide* g, uint32_t n) {
     return std::max(1u, std::min<unsigned>(static_cast<unsigned>(g->sms), (n + 127) / 128));
 }
 
-// Three forward CTAs per SM: one's MMAs overlap the others' epilogues.
+// One persistent forward CTA per SM (its groups share the weights).
 unsigned grid_tiles_fwd(turner_guide* g, uint32_t n) {
-    return std::max(1u, std::min<unsigned>(kFwdBlocksPerSm * static_cast<unsigned>(g->sms), (n + 127) / 128));
+    const unsigned tiles = (n + 127) / 128;
+    return std::max(1u, std::min<unsigned>(static_cast<unsigned>(g->sms), (tiles + kFwdGroups - 1) / kFwdGroups));
 }
 
 } // namespace
