@@ -16,8 +16,8 @@ against the GPU kernels (tests/test_gpu_guide.py).
           p = q/2 + max(0, n.w)/(2 pi) the sampling mixture and n the normal
           of the features: the gradient of sum c^2 p0 / p(params) at p0 = p,
           the second moment of the mixture estimator (variance_objective)
-With bf16=True the GPU's roundings are applied: weights, the encoded input
-and hidden activations to BF16; every layer's output gradient dY to BF16,
+With bf16=True the GPU's roundings are applied: weights, biases, the encoded
+input and hidden activations to BF16; every layer's output gradient dY to BF16,
 as it enters the tensor-core products dY W, dY^T X and the bias sums.
 """
 from __future__ import annotations
@@ -76,7 +76,7 @@ def forward(p: np.ndarray, feat: np.ndarray, use_bf16: bool = False):
     for l, (W, b) in enumerate(layers):
         xs.append(x)
         Wq = bf16(W) if use_bf16 else W
-        y = x @ Wq.T + b
+        y = x @ Wq.T + (bf16(b) if use_bf16 else b)   # the GPU's MMA adds the bias as a BF16 weight
         if l < 4:
             x = np.maximum(y, 0.0)
             if use_bf16:

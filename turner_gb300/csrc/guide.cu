@@ -73,9 +73,8 @@ constexpr uint32_t kFwdTmemCols = 512;   // kFwdGroups x 64 columns, allocated a
 static_assert(kFwdGroups * 64 <= static_cast<int>(kFwdTmemCols), "TMEM columns");
 
 struct FwdSmem {
-    uint8_t act[kFwdGroups][kIn * 128 * 2];   // per group: 128 x 80 inputs, then each layer's 128 x 64 output in place
+    uint8_t act[kFwdGroups][kFwdK * 128 * 2];   // per group: 128 x 80 inputs, then each layer's [128 x 64 output, 1, 0...] in place
     uint8_t w[kFwdBytes];
-    float bias[4 * kHidden + kOut];
     uint64_t mbar[kFwdGroups];
     uint32_t tmem;
 };
@@ -153,10 +152,6 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
     for (int i = tid; i < kFwdBytes / 16; i += kFwdThreads) {
         reinterpret_cast<uint4*>(sm.w)[i] = reinterpret_cast<const uint4*>(wts.fwd)[i];
     }
-    for (int l = 0, o = 0; l < kLayers; ++l) {
-        for (int i = tid; i < layer_out(l); i += kFwdThreads) sm.bias[o + i] = wts.params[layer_b(l) + i];
-        o += layer_out(l);
-    }
     if (tid < kFwdGroups) {
         tc::mbar_init(&sm.mbar[tid], 1);
         tc::fence_mbar_init();
@@ -204,14 +199,16 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
                 if (valid) encode_axis(ax == 0 ? fin[0] : ax == 1 ? fin[1] : fin[2], v);
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
-                    *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 8 * (3 * ax + j), kIn)) = v[j];
+                    *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 8 * (3 * ax + j), kFwdK)) = v[j];
                     if (act_row) act_row[3 * ax + j] = v[j];
                 }
             }
+            // column 78 is the 1 that multiplies layer 1's bias (the stored X_0 keeps 0 there)
             const uint4 v = valid ? make_uint4(pack_bf16x2(fin[3], fin[4]), pack_bf16x2(fin[5], fin[6]),
                                                pack_bf16x2(fin[7], fin[8]), 0u)
                                   : make_uint4(0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 72, kIn)) = v;
+            *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 72, kFwdK)) =
+                make_uint4(v.x, v.y, v.z, pack_bf16x2(1.f, 0.f));
             if (act_row) act_row[9] = v;
         }
         load_features(tile + stride);
@@ -220,15 +217,14 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
         group_sync_or(bar_id, 0);
         tc::tc_fence_after_sync();
 
-        int bias_o = 0;
 #pragma unroll 1
         for (int l = 0; l < kLayers; ++l) {
-            const int K = layer_in(l), N = layer_out_pad(l);
+            const int N = layer_out_pad(l);
             // one thread issues the layer's MMAs and waits for their commit;
             // the rest of the group waits at the barrier, without polling
             bool done = true;
             if (row == 0) {
-                issue_layer(tmem_mma, act, sm.w + fwd_off(l), K, N, mbar);
+                issue_layer(tmem_mma, act, sm.w + fwd_off(l), kFwdK, N, mbar);
                 done = tc::mbar_wait(mbar, phase, err);
             }
             phase ^= 1;
@@ -238,23 +234,26 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
             }
             tc::tc_fence_after_sync();
             if (l < kLayers - 1) {
+                // the MMA has added the bias: ReLU and BF16 packing only
 #pragma unroll 1
                 for (int c0 = 0; c0 < kHidden; c0 += 32) {
                     float v[32];
                     tc::tmem_ld32(tmem + static_cast<uint32_t>(c0), v);
-                    const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const float4 ba = b4[2 * q], bb = b4[2 * q + 1];
-                        const float bq[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
-                        float y[8];
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) y[j] = v[8 * q + j] + bq[j];
-                        const uint4 u = make_uint4(pack_bf16x2_relu(y[0], y[1]), pack_bf16x2_relu(y[2], y[3]),
-                                                   pack_bf16x2_relu(y[4], y[5]), pack_bf16x2_relu(y[6], y[7]));
-                        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, c0 + 8 * q, kHidden)) = u;
+                        const uint4 u = make_uint4(pack_bf16x2_relu(v[8 * q], v[8 * q + 1]),
+                                                   pack_bf16x2_relu(v[8 * q + 2], v[8 * q + 3]),
+                                                   pack_bf16x2_relu(v[8 * q + 4], v[8 * q + 5]),
+                                                   pack_bf16x2_relu(v[8 * q + 6], v[8 * q + 7]));
+                        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, c0 + 8 * q, kFwdK)) = u;
                         if (act_row) act_row[10 + 8 * l + c0 / 8 + q] = u;
                     }
+                }
+                if (l == 0) {
+                    // columns 64-79 of the hidden layers' operand: the 1 of the bias, then zeros
+                    *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 64, kFwdK)) =
+                        make_uint4(pack_bf16x2(1.f, 0.f), 0u, 0u, 0u);
+                    *reinterpret_cast<uint4*>(act + tc::kmajor_offset(row, 72, kFwdK)) = make_uint4(0u, 0u, 0u, 0u);
                 }
             } else {
 #pragma unroll 1
@@ -263,19 +262,13 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(
                     tc::tmem_ld16(tmem + static_cast<uint32_t>(c0), v);   // columns 40-47 are padding
                     if (out && valid) {
                         float4* o4 = reinterpret_cast<float4*>(out + size_t(s) * kOut + c0);
-                        const float4* b4 = reinterpret_cast<const float4*>(sm.bias + bias_o + c0);
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
-                            if (c0 + 4 * q < kOut) {
-                                const float4 b = b4[q];
-                                o4[q] = make_float4(v[4 * q] + b.x, v[4 * q + 1] + b.y, v[4 * q + 2] + b.z,
-                                                    v[4 * q + 3] + b.w);
-                            }
+                            if (c0 + 4 * q < kOut) o4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                         }
                     }
                 }
             }
-            bias_o += layer_out(l);
             tc::fence_async_smem();   // the next layer's MMAs read what this one wrote
             tc::tc_fence_before_sync();
             group_sync_or(bar_id, 0);
@@ -694,16 +687,18 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(
         for (int l = 0; l < kLayers; ++l) {
             const int K = layer_in(l), nout = layer_out(l), pad = layer_out_pad(l);
             const float* W = adam.params + layer_w(l);
+            for (int e = tid; e < pad * kFwdK; e += kBwdThreads) {
+                const int r = e / kFwdK, k = e - r * kFwdK;
+                store_bf16(adam.fwd + fwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(r), static_cast<uint32_t>(k),
+                                                                    static_cast<uint32_t>(kFwdK)),
+                           fwd_operand(adam.params, l, r, k));
+            }
+            if (l == 0) continue;
             for (int e = tid; e < pad * K; e += kBwdThreads) {
                 const int r = e / K, k = e - r * K;
                 const float w = r < nout ? W[r * K + k] : 0.f;
-                store_bf16(adam.fwd + fwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(r), static_cast<uint32_t>(k),
-                                                                    static_cast<uint32_t>(K)), w);
-                if (l > 0) {
-                    store_bf16(adam.bwd + bwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(k),
-                                                                        static_cast<uint32_t>(r),
-                                                                        static_cast<uint32_t>(pad)), w);
-                }
+                store_bf16(adam.bwd + bwd_off(l), tc::kmajor_offset(static_cast<uint32_t>(k), static_cast<uint32_t>(r),
+                                                                    static_cast<uint32_t>(pad)), w);
             }
         }
     }
@@ -735,13 +730,15 @@ __global__ void k_pack(const float* __restrict__ p, uint8_t* __restrict__ fwd, u
     const int l = blockIdx.y;
     const int K = layer_in(l), out = layer_out(l), pad = layer_out_pad(l);
     const float* W = p + layer_w(l);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < pad * kFwdK; e += gridDim.x * blockDim.x) {
+        const int r = e / kFwdK, k = e - r * kFwdK;   // forward: row = output, column = input (+ bias)
+        store_bf16(fwd + fwd_off(l), tc::kmajor_offset(r, k, kFwdK), fwd_operand(p, l, r, k));
+    }
+    if (l == 0) return;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < pad * K; e += gridDim.x * blockDim.x) {
-        const int r = e / K, k = e - r * K;   // forward: row = output, column = input
+        const int r = e / K, k = e - r * K;   // backward: row = input k, column = output r
         const float w = r < out ? W[r * K + k] : 0.f;
-        store_bf16(fwd + fwd_off(l), tc::kmajor_offset(r, k, K), w);
-        if (l > 0) {                          // backward: row = input k, column = output r
-            store_bf16(bwd + bwd_off(l), tc::kmajor_offset(k, r, pad), w);
-        }
+        store_bf16(bwd + bwd_off(l), tc::kmajor_offset(k, r, pad), w);
     }
 }
 

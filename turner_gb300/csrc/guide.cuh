@@ -36,13 +36,25 @@ __host__ __device__ constexpr int layer_w(int l) { return l == 0 ? kW1 : l == 1 
 __host__ __device__ constexpr int layer_b(int l) { return l == 0 ? kB1 : l == 1 ? kB2 : l == 2 ? kB3 : l == 3 ? kB4 : kB5; }
 
 // Packed BF16 operand tiles (core-matrix K-major, see tc.cuh), in bytes:
-//   forward  W_l as [out_pad x in]      (B operand of X * W^T)
-//   backward W_l^T as [in x out_pad]    (B operand of dY * W), layers 2-5 only
-__host__ __device__ constexpr int fwd_bytes(int l) { return layer_out_pad(l) * layer_in(l) * 2; }
+//   forward  [W_l | b_l] as [out_pad x 80]  (B operand of [X, 1] * [W, b]^T):
+//            the bias sits in column fwd_bias_col(l) (layer 1: column 78,
+//            the first padding column of the encoded input; the others:
+//            column 64, after the 64 hidden inputs), where the forward's
+//            operand A holds 1; the other columns past the inputs are zero
+//   backward W_l^T as [in x out_pad]        (B operand of dY * W), layers 2-5 only
+constexpr int kFwdK = 80;
+__host__ __device__ constexpr int fwd_bias_col(int l) { return l == 0 ? kInUsed : kHidden; }
+__host__ __device__ constexpr int fwd_bytes(int l) { return layer_out_pad(l) * kFwdK * 2; }
 __host__ __device__ constexpr int fwd_off(int l) {
     return l == 0 ? 0 : fwd_off(l - 1) + fwd_bytes(l - 1);
 }
-constexpr int kFwdBytes = fwd_off(kLayers);                      // 40,960
+constexpr int kFwdBytes = fwd_off(kLayers);                      // 48,640
+// Element (r, k) of layer l's forward operand from the FP32 parameters.
+__host__ __device__ inline float fwd_operand(const float* params, int l, int r, int k) {
+    if (r >= layer_out(l)) return 0.f;
+    if (k == fwd_bias_col(l)) return params[layer_b(l) + r];
+    return k < layer_in(l) ? params[layer_w(l) + r * layer_in(l) + k] : 0.f;
+}
 __host__ __device__ constexpr int bwd_bytes(int l) { return l == 0 ? 0 : layer_in(l) * layer_out_pad(l) * 2; }
 __host__ __device__ constexpr int bwd_off(int l) {
     return l == 0 ? 0 : bwd_off(l - 1) + bwd_bytes(l - 1);
