@@ -1,16 +1,19 @@
 // Learned bounce proposal: the MLP's forward, backward and Adam kernels.
 //
-// Forward (k_mlp_forward): persistent CTAs of 256 threads (three per SM)
-// take tiles of 128 samples, two threads per sample. The encoded inputs and
-// every hidden activation stay in shared memory as BF16 in the core-matrix
-// K-major layout (tc.cuh), one buffer updated in place; thread 0 issues
-// tcgen05.mma (M = 128, N = 64 or 48, K in steps of 16) into a TMEM
-// accumulator, commits to an mbarrier, and each warp reads its 32 lanes and
-// half of the columns back with tcgen05.ld to add the bias, apply ReLU and
-// write the next layer's operand with 16-byte stores.
+// Forward (k_mlp_forward): one persistent CTA per SM, six warpgroups, each
+// an independent pipeline over tiles of 128 samples (one thread per sample)
+// that shares the CTA's packed weights. The encoded inputs and every hidden
+// activation stay in the group's shared-memory buffer as BF16 in the
+// core-matrix K-major layout (tc.cuh), updated in place, with a column of
+// ones that multiplies the bias column of the weights; the group's thread 0
+// issues tcgen05.mma (M = 128, N = 64 or 48, K = 80 in steps of 16) into the
+// group's 64 TMEM columns and waits for the commit, and each thread reads its
+// row back with tcgen05.ld, applies ReLU with the BF16 conversion and writes
+// the next layer's operand with 16-byte stores.
 //
 // Backward (k_mlp_backward): per tile, the vMF-mixture head gradient of the
-// loss -c log q(w) (one thread per sample), then per layer from the top, on
+// loss -c log q(w) (one thread per sample; the variance objective reweights
+// it), then per layer from the top, on
 // the tensor cores: dX = dY W (a second BF16 copy of the weights,
 // transposed), masked by ReLU', and [dW, db] += dY^T [X, 1] accumulated in
 // TMEM over all of a CTA's tiles. Each CTA adds its gradient to the global one
