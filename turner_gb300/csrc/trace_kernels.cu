@@ -286,9 +286,17 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                     const bool guided = job.sampling == kSamplingGuided && depth < job.guide_depth;
                     if (guided) {
                         // learned proposal: 1/2 cosine about the normal, 1/2 the vMF mixture
+                        // the network's 40 outputs of this hit: 160 bytes, read once as float4
                         float raw[guide::kOut];
+                        const float4* o4 = reinterpret_cast<const float4*>(gq.out + guide::kOut * size_t(i));
 #pragma unroll
-                        for (int k = 0; k < guide::kOut; ++k) raw[k] = gq.out[guide::kOut * size_t(i) + k];
+                        for (int k = 0; k < guide::kOut / 4; ++k) {
+                            const float4 v = __ldcs(o4 + k);
+                            raw[4 * k] = v.x;
+                            raw[4 * k + 1] = v.y;
+                            raw[4 * k + 2] = v.z;
+                            raw[4 * k + 3] = v.w;
+                        }
                         guide::Mixture mix;
                         guide::decode(raw, mix);
                         const float u_sel = xorshift_float(rs);
@@ -305,12 +313,25 @@ __global__ void __launch_bounds__(kBlock) k_shade(const JobDesc* __restrict__ jo
                             w3[1] = m[3] * xx + m[4] * yy + m[5] * zz;
                             w3[2] = m[6] * xx + m[7] * yy + m[8] * zz;
                         } else {
-                            int l = 0;
-                            float acc = mix.w[0];
-                            while (l < guide::kLobes - 1 && uc > acc) acc += mix.w[++l];
+                            // the first lobe whose cumulative weight reaches uc (the
+                            // last one if rounding leaves the sum short), picked with
+                            // static indices so that the mixture stays in registers
+                            float sel[3] = {0.f, 0.f, 1.f}, sel_kappa = 1.f, acc = 0.f;
+                            bool found = false;
+#pragma unroll
+                            for (int l = 0; l < guide::kLobes; ++l) {
+                                acc += mix.w[l];
+                                if (!found && (uc <= acc || l == guide::kLobes - 1)) {
+                                    sel[0] = mix.mu[l][0];
+                                    sel[1] = mix.mu[l][1];
+                                    sel[2] = mix.mu[l][2];
+                                    sel_kappa = mix.kappa[l];
+                                    found = true;
+                                }
+                            }
                             float rot[9];
-                            from_to_z(make_float3(mix.mu[l][0], mix.mu[l][1], mix.mu[l][2]), rot);
-                            guide::vmf_sample(mix.mu[l], mix.kappa[l], ua, ub, rot, w3);
+                            from_to_z(make_float3(sel[0], sel[1], sel[2]), rot);
+                            guide::vmf_sample(sel, sel_kappa, ua, ub, rot, w3);
                         }
                         const float cw = nrm.x * w3[0] + nrm.y * w3[1] + nrm.z * w3[2];
                         const float pdf = 0.5f * guide::mixture_pdf(mix, w3) + 0.5f * fmaxf(cw, 0.f) * guide::kInvPi;
