@@ -86,6 +86,7 @@ struct turner_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<std::unique_ptr<SceneStore>> scenes;
+    std::vector<uint32_t> validate_scratch;   // node-check depths of the last upload, kept for the next
     // render workspace
     PinnedBuf staging;                 // upload staging (scene records)
     DevBuf L, qa[4], qb[4], hits, shq[3], shjob, shaux, counters, image, rays_in, rays_out, work, jobtab, jobcnt, acc, tune_out;
@@ -183,9 +184,9 @@ void collect_kernel_times(turner_ctx* ctx) {
 // or -1. Every edge of the flattened tree points forward (left child i + 1,
 // right child > i, next leaf of a run i + 1), so one forward pass that only
 // looks at nodes reached from the root visits them after all their parents.
-long validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris) {
+long validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris, std::vector<uint32_t>& depth) {
     if (n_nodes == 0) return -1;
-    std::vector<uint32_t> depth(n_nodes, 0);    // inner nodes above, +1 (0: not reached)
+    depth.assign(n_nodes, 0);    // inner nodes above, +1 (0: not reached); reused, so no fresh pages per call
     depth[0] = 1;
     uint32_t height = 0;
     for (uint32_t i = 0; i < n_nodes; ++i) {
@@ -372,7 +373,8 @@ const char* turner_last_error_message(turner_ctx* ctx) { return ctx ? ctx->last_
 
 int turner_validate_nodes(const uint64_t* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t* stack_depth) {
     if (!nodes || n_nodes == 0 || n_tris == 0) return TURNER_ERR_INVALID_ARG;
-    const long depth = validate_nodes(nodes, n_nodes, n_tris);
+    std::vector<uint32_t> scratch;
+    const long depth = validate_nodes(nodes, n_nodes, n_tris, scratch);
     if (depth < 0) return TURNER_ERR_BAD_SCENE;
     if (stack_depth) *stack_depth = static_cast<uint32_t>(depth);
     return depth > kStackCap ? TURNER_ERR_TOO_LARGE : TURNER_OK;
@@ -384,7 +386,9 @@ int turner_upload_scene(turner_ctx* ctx, const uint64_t* nodes, uint32_t n_nodes
     if (n_tris >= TURNER_MISS || n_nodes >= TURNER_MISS) return TURNER_ERR_TOO_LARGE;
     TURNER_CK(cudaSetDevice(ctx->device));
     // the node check runs on its own thread while the records are converted
-    auto checked = std::async(std::launch::async, [=]() { return validate_nodes(nodes, n_nodes, n_tris); });
+    std::vector<uint32_t>& scratch = ctx->validate_scratch;
+    auto checked = std::async(std::launch::async,
+                              [=, &scratch]() { return validate_nodes(nodes, n_nodes, n_tris, scratch); });
     auto fail = [&](int status) {
         checked.wait();
         return status;
