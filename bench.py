@@ -652,7 +652,8 @@ def main() -> None:
     ap.add_argument("--pass-spp", type=int, default=1)
     ap.add_argument("--budget", type=float, default=10.0)
     ap.add_argument("--ref-cache", default="", help="guide: .npz file that keeps the FP64 reference between runs")
-    ap.add_argument("--train-fraction", type=float, default=0.2)
+    ap.add_argument("--train-fraction", type=float, default=0.1,
+                    help="guide: share of the budget the learned tracer trains for (its passes count toward its image)")
     ap.add_argument("--guide-records", type=int, default=1 << 18)
     ap.add_argument("--guide-lr", type=float, default=1e-3)
     ap.add_argument("--guide-steps", type=int, default=16, help="Adam steps per training pass")
