@@ -587,7 +587,7 @@ def run_views16(args) -> None:
             ctx.set_guide(g2, train=True, lr=args.guide_lr, records=args.guide_records,
                           steps_per_pass=args.guide_steps)
             learned, learned_spp, learned_s = accumulate(tg.SAMPLING_GUIDED, args.pass_spp, seed, budget=args.budget,
-                                                         train_fraction=args.train_fraction, guide=g2)
+                                                         train_fraction=args.views_train_fraction, guide=g2)
             ctx.set_guide(None)
             g2.close()
             m_plain = float(((plain - ref) ** 2).mean())
@@ -610,7 +610,8 @@ def run_views16(args) -> None:
         "throughput_clocks": thr_clk.summary,
         "equal_time": {"views": f"16 x 1920x1080, rows {band[0]}-{band[1]} of each (crop: a 16k-spp reference "
                                 f"of whole frames would take hours)",
-                       "budget_s": args.budget, "reference_spp": 2 * half * 64,
+                       "budget_s": args.budget, "train_fraction": args.views_train_fraction,
+                       "reference_spp": 2 * half * 64,
                        "reference_s": round(ref_s, 1), "reference_variance": ref_var,
                        "mse_ratio": round(float(np.mean(ratios)), 4), "min": min(ratios), "max": max(ratios),
                        "std": round(float(np.std(ratios)), 4),
@@ -645,6 +646,9 @@ def main() -> None:
     ap.add_argument("--views-train-s", type=float, default=3.0)
     ap.add_argument("--views-ref-spp", type=int, default=16384)
     ap.add_argument("--views-eq-rows", type=int, default=8, help="views16: rows of each view in the equal-time crop")
+    ap.add_argument("--views-train-fraction", type=float, default=0.2,
+                    help="views16: share of the equal-time budget the learned tracer trains for (measured best: 0.2 "
+                         "here, 0.1 for the single view)")
     # guide workload defaults: the indirect-lit room at 1024x1024 against a
     # 16,384-spp FP64 reference, 10 s of equal wall time in 1-spp passes
     ap.add_argument("--guide-side", type=int, default=1024)
