@@ -113,9 +113,9 @@ __device__ __forceinline__ uint32_t pack_bf16x2_relu(float lo, float hi) {
 // The 24 encoded inputs of one coordinate (see encode()): (sin, cos) of
 // pi 2^i x for i = 0..11, as three groups of eight BF16. One sincospif, then
 // the double-angle identities sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)
-// (cos a + sin a): eleven doublings grow the FP32 error to at most 2^11 times
-// sincospif's (about 1e-4), a twentieth of the BF16 rounding of the stored
-// value (2^-9).
+// (cos a + sin a): eleven doublings grow the FP32 error to about 2^11 times
+// sincospif's (2e-4 at the highest frequency, emulated in FP32), a tenth of
+// the BF16 rounding of the stored value (2^-9 relative).
 __device__ __forceinline__ void encode_axis(float x, uint4 out[3]) {
     float sn, cs;
     sincospif(x, &sn, &cs);
